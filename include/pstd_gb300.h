@@ -1,0 +1,207 @@
+/*
+ * pstd_gb300.h -- C ABI of the GB300-native PSTD solve.
+ *
+ * This is the drop-in boundary for openPSTD's kernel API.  Every entry point
+ * replaces one piece of the reference's C++ interface (paths are relative to
+ * the openPSTD source tree):
+ *
+ *   pstd_create          <- PSTDKernel::initialize_kernel   (kernel/PSTDKernel.cpp:49-59)
+ *   pstd_run             <- PSTDKernel::run + GPUSingleThreadSolver::compute_propagation
+ *                           (kernel/PSTDKernel.cpp:121-148, kernel/Solver.cpp:62-93,153-156)
+ *   pstd_get_metadata    <- PSTDKernel::get_metadata        (kernel/PSTDKernel.cpp:154-168)
+ *   pstd_destroy         <- ~PSTDKernel
+ *   pstd_callbacks       <- KernelCallback / KernelCallbackLog (kernel/KernelInterface.h:243-304)
+ *   pstd_config          <- PSTDConfiguration / PSTDSettings / DomainConf
+ *                           (kernel/KernelInterface.h:44-240)
+ *
+ * Extra entry points (device-resident stepping, snapshots, scene inspection,
+ * batched multi-scene solves and the serving loop) have no single reference
+ * counterpart; each says so.
+ *
+ * Conventions: every function returns an int status (PSTD_OK == 0); no C++
+ * exception crosses this boundary.  pstd_last_error() gives a message for the
+ * last failing call on the calling thread.  All pointers are host pointers
+ * unless a parameter name says "dev".  Grid axes follow the reference: x is
+ * the column index, y the row index, fields are stored row-major (x fastest)
+ * when they cross this boundary.
+ */
+#ifndef PSTD_GB300_H
+#define PSTD_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define PSTD_OK                 0
+#define PSTD_ERR_INVALID        1  /* bad argument or malformed configuration */
+#define PSTD_ERR_NOT_CONFIGURED 2  /* PSTDKernelNotConfiguredException (kernel/PSTDKernel.cpp:122-123) */
+#define PSTD_ERR_CUDA           3  /* a CUDA runtime call failed */
+#define PSTD_ERR_UNSUPPORTED    4  /* scene makes the reference read undefined memory (see message) */
+#define PSTD_ERR_CALLBACK       5  /* a callback returned non-zero: run stopped between frames */
+#define PSTD_ERR_NO_MEMORY      6  /* device or pinned host allocation failed / over budget */
+#define PSTD_ERR_CANCELLED      7  /* request cancelled */
+#define PSTD_ERR_TIMEOUT        8  /* a bounded device wait gave up */
+
+/* ---- log levels (KernelCallbackLog, kernel/KernelInterface.h:243-271) --- */
+#define PSTD_LOG_FATAL   0
+#define PSTD_LOG_ERROR   1
+#define PSTD_LOG_WARNING 2
+#define PSTD_LOG_INFO    3
+#define PSTD_LOG_DEBUG   4
+
+/* ---- configuration (PSTDSettings, kernel/KernelInterface.h:44-158) ----- */
+typedef struct pstd_settings {
+    float calctime;        /* render time [s]                         */
+    float c1;              /* sound speed [m/s]                       */
+    float ampMax;          /* PML attenuation coefficient             */
+    float freqMax;         /* maximum frequency (not used by the solve) */
+    float rho;             /* density of air [kg/m^3]                 */
+    float patcherror;      /* patch error [dB]; sets window size      */
+    float tfactRK;         /* CFL factor; dt = tfactRK*dx/c1          */
+    float gridSpacing;     /* dx = dy [m]                             */
+    float band_width;      /* Gaussian speaker band width [1/m^2]     */
+    float wave_length;     /* (only used by spectral interpolation)   */
+    float rk_coefficients[6];
+    int32_t n_rk_coefficients;     /* must be 6 */
+    int32_t spectral_interpolation;/* ignored: the reference hard-disables it (kernel/core/Receiver.cpp:48) */
+    int32_t PMLCells;
+    int32_t SaveNth;
+} pstd_settings;
+
+/* DomainConfEdge (kernel/KernelInterface.h:163-175) */
+typedef struct pstd_domain_edge {
+    float absorption;
+    int32_t lr;            /* locally reacting flag */
+} pstd_domain_edge;
+
+/* DomainConf (kernel/KernelInterface.h:180-205); world units [m] */
+typedef struct pstd_domain_conf {
+    float top_left[2];
+    float size[2];
+    pstd_domain_edge T, L, B, R;
+} pstd_domain_conf;
+
+/* PSTDConfiguration (kernel/KernelInterface.h:213-240) */
+typedef struct pstd_config {
+    pstd_settings settings;
+    int32_t n_domains;
+    const pstd_domain_conf* domains;
+    int32_t n_speakers;
+    const float* speakers;   /* 3*n_speakers floats, world (x, y, z) */
+    int32_t n_receivers;
+    const float* receivers;  /* 3*n_receivers floats, world (x, y, z) */
+} pstd_config;
+
+/* ---- callbacks (KernelCallback, kernel/KernelInterface.h:279-304) ------- */
+/* write_frame: data is row-major (x fastest), n = Nx*Ny floats of p0 of a
+ *   non-PML domain, valid only for the duration of the call (copy to keep).
+ *   Called when frame % SaveNth == 0, before PML attenuation (kernel/Solver.cpp:80-84).
+ * write_sample: n == 1 sample of receiver `receiver` at time step start_sample
+ *   (kernel/Solver.cpp:86-91).
+ * A non-zero return stops the run at the next frame boundary with
+ * PSTD_ERR_CALLBACK.  log may be NULL. */
+typedef struct pstd_callbacks {
+    void* user;
+    int (*write_frame)(void* user, int32_t frame, int32_t domain, const float* data, int64_t n);
+    int (*write_sample)(void* user, int32_t start_sample, int32_t receiver, const float* data, int64_t n);
+    void (*log)(void* user, int32_t level, const char* message);
+} pstd_callbacks;
+
+typedef struct pstd_kernel pstd_kernel;
+
+/* Build the scene (domains, automatic PML, speakers, receivers, attenuation
+ * tables) on the host and upload it to device 0.
+ * Replaces PSTDKernel::initialize_kernel (kernel/PSTDKernel.cpp:49-70). */
+int pstd_create(const pstd_config* config, const pstd_callbacks* log_cb, pstd_kernel** out);
+
+/* Replaces PSTDKernel::~PSTDKernel. Safe on NULL. */
+void pstd_destroy(pstd_kernel* k);
+
+/* Replaces PSTDKernel::get_metadata (kernel/PSTDKernel.cpp:154-168).
+ * dims receives 3 ints (x, y, z=0) per scene domain, PML included, in scene
+ * order; at most `cap` domains are written, *n_domains gets the total. */
+int pstd_get_metadata(pstd_kernel* k, int32_t* n_domains, int32_t* dims, int32_t cap, int32_t* framecount);
+
+/* Replaces PSTDKernel::run with the GPU solver (kernel/PSTDKernel.cpp:121-148,
+ * kernel/Solver.cpp:62-93).  Runs Framecount time steps from the current
+ * state, emitting frames and receiver samples through cb.  Blocks the
+ * calling thread; callbacks run on it, in frame order. */
+int pstd_run(pstd_kernel* k, const pstd_callbacks* cb);
+
+/* ---- device-resident stepping (no reference counterpart) --------------- */
+/* Advance n_steps time steps on `stream` (a cudaStream_t, NULL = the handle's
+ * own stream) without callbacks.  Receiver samples are kept on the device
+ * (readable with pstd_get_receivers).  Asynchronous: returns after enqueue. */
+int pstd_advance(pstd_kernel* k, int32_t n_steps, void* stream);
+
+/* Re-initialise the fields to the state right after pstd_create (speaker
+ * initial condition, zero velocities, step counter 0). Asynchronous on the
+ * handle's stream. */
+int pstd_reset(pstd_kernel* k);
+
+/* Synchronise the handle's stream. */
+int pstd_synchronize(pstd_kernel* k);
+
+/* Number of time steps taken so far. */
+int pstd_steps_done(pstd_kernel* k, int32_t* steps);
+
+/* Copy receiver samples [first_step, first_step+n_steps) x n_receivers into
+ * dst (step-major).  Only steps taken since the last pstd_reset that are
+ * still in the device ring (capacity set at create: Framecount) are valid. */
+int pstd_get_receivers(pstd_kernel* k, int32_t first_step, int32_t n_steps, float* dst);
+
+/* Field codes for pstd_snapshot */
+#define PSTD_FIELD_P0 0
+#define PSTD_FIELD_PX 1
+#define PSTD_FIELD_PY 2
+#define PSTD_FIELD_VX 3   /* Ny x (Nx+1) */
+#define PSTD_FIELD_VY 4   /* (Ny+1) x Nx */
+
+/* Copy one field of scene domain `domain_index` (scene order, PML included)
+ * to dst, row-major, dense.  n must equal the field's element count. */
+int pstd_snapshot(pstd_kernel* k, int32_t domain_index, int32_t field, float* dst, int64_t n);
+
+/* ---- scene inspection (no reference counterpart; used for parity tests) - */
+typedef struct pstd_domain_info {
+    int32_t id;
+    int32_t top_left[2];
+    int32_t size[2];
+    int32_t is_pml, is_secondary_pml, is_rigid, local;
+    int32_t should_update[2];       /* [X, Y] */
+    int32_t n_neighbours[4];        /* LEFT, RIGHT, TOP, BOTTOM (kernel/core/kernel_functions.h:94-96) */
+    int32_t fft_length[2];          /* X, Y strip transform length (0 if not updated) */
+    int32_t window[2];              /* window length after halving, X, Y */
+    float alpha, impedance, rho;
+} pstd_domain_info;
+
+int pstd_scene_domain_count(pstd_kernel* k, int32_t* n);
+int pstd_scene_domain_info(pstd_kernel* k, int32_t index, pstd_domain_info* out);
+/* dir: 0 LEFT 1 RIGHT 2 TOP 3 BOTTOM; writes scene indices of the neighbours */
+int pstd_scene_neighbours(pstd_kernel* k, int32_t index, int32_t dir, int32_t* out, int32_t cap, int32_t* n);
+/* PML attenuation vectors of a domain: ax_p[Nx], ax_v[Nx+1], ay_p[Ny], ay_v[Ny+1]
+ * (1 where the domain is not attenuated along that axis). */
+int pstd_scene_attenuation(pstd_kernel* k, int32_t index, float* ax_p, float* ax_v, float* ay_p, float* ay_v);
+
+/* ---- timing of the strip-derivative passes (no reference counterpart) --- */
+/* Advance n_steps with CUDA events around every pass launch; returns the summed
+ * device time [ms] of the x-direction and y-direction passes and the number of
+ * launches of each.  Results are identical to pstd_advance. */
+int pstd_profile_passes(pstd_kernel* k, int32_t n_steps, void* stream,
+                        float* ms_x, float* ms_y, int32_t* launches_x, int32_t* launches_y);
+
+/* Counts that define the work: cells advanced per step (pressure cells of
+ * non-rigid domains), of which air cells, and the number of kernel launches
+ * per time step. */
+int pstd_work_counts(pstd_kernel* k, int64_t* cells, int64_t* air_cells, int32_t* launches_per_step);
+
+/* ---- library ------------------------------------------------------------ */
+const char* pstd_last_error(void);
+const char* pstd_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PSTD_GB300_H */

@@ -1,0 +1,252 @@
+"""openPSTD's kernel API on the GB300 solver.
+
+Mirrors ``KernelCallbackLog``, ``KernelCallback``, ``SimulationMetadata``,
+``KernelInterface``, ``PSTDKernelNotConfiguredException`` and ``PSTDKernel``
+(kernel/KernelInterface.h:243-361, kernel/PSTDKernel.h:52-150) with the same
+method names and semantics:
+
+* ``initialize_kernel(config, callbackLog)`` builds the scene (on the device);
+* ``run(callback)`` advances Framecount time steps and calls
+  ``WriteFrame(frame, domain, data)`` for every non-PML domain and
+  ``WriteSample(frame, receiver, [p])`` for every receiver when
+  ``frame % SaveNth == 0``, in frame order, on the calling thread;
+* ``get_metadata()`` lists {Nx, Ny, 0} for every scene domain (PML included)
+  and the frame count;
+* ``run``/``get_metadata`` before ``initialize_kernel`` raise
+  ``PSTDKernelNotConfiguredException`` (kernel/PSTDKernel.cpp:122-123,155-156).
+
+Frames are numpy float32 arrays of length Nx*Ny, row-major with x fastest
+(kernel/Solver.cpp:208-217); the callee may keep them.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import List, Optional
+
+import numpy as np
+
+from . import _lib
+from .config import CConfig, PSTDConfiguration, c_domain_info
+
+LOG_LEVELS = ("Fatal", "Error", "Warning", "Info", "Debug")
+
+
+class KernelCallbackLog:
+    """kernel/KernelInterface.h:243-271; every method is a non-blocking no-op by default."""
+
+    def Fatal(self, message: str): pass
+    def Error(self, message: str): pass
+    def Warning(self, message: str): pass
+    def Info(self, message: str): pass
+    def Debug(self, message: str): pass
+
+
+class KernelCallback(KernelCallbackLog):
+    """kernel/KernelInterface.h:279-304."""
+
+    def Callback(self, status, message: str, frame: int):   # deprecated in the reference
+        pass
+
+    def WriteFrame(self, frame: int, domain: int, data: np.ndarray):
+        raise NotImplementedError
+
+    def WriteSample(self, startSample: int, receiver: int, data: List[float]):
+        raise NotImplementedError
+
+
+class SimulationMetadata:
+    """kernel/KernelInterface.h:309-329."""
+
+    def __init__(self):
+        self.DomainMetadata: List[List[int]] = []
+        self.Framecount = 0
+        self.DomainPositions: List[List[int]] = []
+
+
+class PSTDKernelNotConfiguredException(Exception):
+    def __str__(self):
+        return "The kernel is not yet configured"
+
+
+class KernelInterface:
+    """kernel/KernelInterface.h:332-351."""
+
+    def initialize_kernel(self, config: PSTDConfiguration, callbackLog: KernelCallbackLog): raise NotImplementedError
+    def run(self, callback: KernelCallback): raise NotImplementedError
+    def get_metadata(self) -> SimulationMetadata: raise NotImplementedError
+
+
+def _log_bridge(target: Optional[KernelCallbackLog]):
+    def _log(user, level, msg):
+        if target is None:
+            return
+        name = LOG_LEVELS[level] if 0 <= level < len(LOG_LEVELS) else "Debug"
+        try:
+            getattr(target, name)(msg.decode())
+        except Exception:   # log callbacks must not break the run
+            pass
+    return _lib.LOG(_log)
+
+
+class PSTDKernel(KernelInterface):
+    """GPU solver behind the reference's PSTDKernel interface.
+
+    ``GPU`` must be true: this package provides the GPU branch of
+    ``PSTDKernel::run`` (kernel/PSTDKernel.cpp:126-141) and has no CPU
+    solver.  ``MCPU`` is accepted for signature compatibility and ignored.
+    """
+
+    def __init__(self, GPU: bool = True, MCPU: bool = False):
+        if not GPU:
+            raise ValueError("openpstd_gb300 provides the GPU solver only (PSTDKernel(GPU=True))")
+        self.GPU, self.MCPU = GPU, MCPU
+        self._h = None
+        self._cfg: Optional[PSTDConfiguration] = None
+        self._keep = []
+
+    # ---- reference API ---------------------------------------------------
+    def initialize_kernel(self, config: PSTDConfiguration, callbackLog: Optional[KernelCallbackLog] = None):
+        L = _lib.lib()
+        self.close()
+        self._cfg = config.copy()
+        self._cc = CConfig(self._cfg)
+        logcb = _log_bridge(callbackLog)
+        cbs = _lib.c_callbacks(None, _lib.WRITE_FRAME(), _lib.WRITE_SAMPLE(), logcb)
+        h = ctypes.c_void_p()
+        rc = L.pstd_create(ctypes.byref(self._cc.c), ctypes.byref(cbs), ctypes.byref(h))
+        _lib.check(rc)
+        self._h = h
+        self._keep = [logcb, cbs]
+
+    def run(self, callback: KernelCallback):
+        h = self._need()
+        errors = []
+
+        def _frame(user, frame, domain, data, n):
+            try:
+                callback.WriteFrame(int(frame), int(domain), np.ctypeslib.as_array(data, shape=(n,)).copy())
+                return 0
+            except Exception as e:   # stop the run, re-raise after it returns
+                errors.append(e)
+                return 1
+
+        def _sample(user, start, rec, data, n):
+            try:
+                callback.WriteSample(int(start), int(rec), [float(data[i]) for i in range(n)])
+                return 0
+            except Exception as e:
+                errors.append(e)
+                return 1
+
+        fcb, scb, lcb = _lib.WRITE_FRAME(_frame), _lib.WRITE_SAMPLE(_sample), _log_bridge(callback)
+        cbs = _lib.c_callbacks(None, fcb, scb, lcb)
+        rc = _lib.lib().pstd_run(h, ctypes.byref(cbs))
+        if errors:
+            raise errors[0]
+        _lib.check(rc)
+
+    def get_metadata(self) -> SimulationMetadata:
+        h = self._need()
+        n = ctypes.c_int32()
+        fc = ctypes.c_int32()
+        _lib.check(_lib.lib().pstd_get_metadata(h, ctypes.byref(n), None, 0, ctypes.byref(fc)))
+        dims = (ctypes.c_int32 * (3 * n.value))()
+        _lib.check(_lib.lib().pstd_get_metadata(h, ctypes.byref(n), dims, n.value, ctypes.byref(fc)))
+        md = SimulationMetadata()
+        md.DomainMetadata = [[dims[3 * i], dims[3 * i + 1], dims[3 * i + 2]] for i in range(n.value)]
+        md.Framecount = fc.value
+        return md
+
+    # ---- device-resident extras -----------------------------------------
+    def _need(self):
+        if self._h is None:
+            raise PSTDKernelNotConfiguredException()
+        return self._h
+
+    def close(self):
+        if self._h is not None:
+            _lib.lib().pstd_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._need()
+
+    def advance(self, n_steps: int, stream: Optional[int] = None):
+        """Enqueue n_steps time steps (no callbacks); stream is a cudaStream_t handle or None."""
+        _lib.check(_lib.lib().pstd_advance(self._need(), int(n_steps), ctypes.c_void_p(stream) if stream else None))
+
+    def reset(self):
+        _lib.check(_lib.lib().pstd_reset(self._need()))
+
+    def synchronize(self):
+        _lib.check(_lib.lib().pstd_synchronize(self._need()))
+
+    def steps_done(self) -> int:
+        n = ctypes.c_int32()
+        _lib.check(_lib.lib().pstd_steps_done(self._need(), ctypes.byref(n)))
+        return n.value
+
+    def receivers(self, first: int = 0, n_steps: Optional[int] = None) -> np.ndarray:
+        done = self.steps_done()
+        n_steps = done - first if n_steps is None else n_steps
+        nrec = len(self._cfg.Receivers)
+        out = np.zeros((n_steps, nrec), dtype=np.float32)
+        if nrec and n_steps:
+            _lib.check(_lib.lib().pstd_get_receivers(self._need(), first, n_steps,
+                                                     out.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+        return out
+
+    def domain_count(self) -> int:
+        n = ctypes.c_int32()
+        _lib.check(_lib.lib().pstd_scene_domain_count(self._need(), ctypes.byref(n)))
+        return n.value
+
+    def domain_info(self, i: int) -> dict:
+        d = c_domain_info()
+        _lib.check(_lib.lib().pstd_scene_domain_info(self._need(), i, ctypes.byref(d)))
+        return d.as_dict()
+
+    def neighbours(self, i: int, direction: int) -> List[int]:
+        buf = (ctypes.c_int32 * 256)()
+        n = ctypes.c_int32()
+        _lib.check(_lib.lib().pstd_scene_neighbours(self._need(), i, direction, buf, 256, ctypes.byref(n)))
+        return [buf[k] for k in range(n.value)]
+
+    def attenuation(self, i: int):
+        d = self.domain_info(i)
+        nx, ny = d["size"]
+        arrs = [np.zeros(nx, np.float32), np.zeros(nx + 1, np.float32), np.zeros(ny, np.float32),
+                np.zeros(ny + 1, np.float32)]
+        P = ctypes.POINTER(ctypes.c_float)
+        _lib.check(_lib.lib().pstd_scene_attenuation(self._need(), i, *[a.ctypes.data_as(P) for a in arrs]))
+        return arrs
+
+    def snapshot(self, i: int, field: str) -> np.ndarray:
+        d = self.domain_info(i)
+        nx, ny = d["size"]
+        shape = {"p0": (ny, nx), "px": (ny, nx), "py": (ny, nx), "vx": (ny, nx + 1), "vy": (ny + 1, nx)}[field]
+        out = np.zeros(shape, dtype=np.float32)
+        _lib.check(_lib.lib().pstd_snapshot(self._need(), i, _lib.FIELD[field],
+                                            out.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), out.size))
+        return out
+
+    def profile_passes(self, n_steps: int, stream: Optional[int] = None):
+        mx, my = ctypes.c_float(), ctypes.c_float()
+        lx, ly = ctypes.c_int32(), ctypes.c_int32()
+        _lib.check(_lib.lib().pstd_profile_passes(self._need(), int(n_steps), ctypes.c_void_p(stream) if stream else None,
+                                                  ctypes.byref(mx), ctypes.byref(my), ctypes.byref(lx),
+                                                  ctypes.byref(ly)))
+        return {"ms_x": mx.value, "ms_y": my.value, "launches_x": lx.value, "launches_y": ly.value}
+
+    def work_counts(self):
+        c, a = ctypes.c_int64(), ctypes.c_int64()
+        l_ = ctypes.c_int32()
+        _lib.check(_lib.lib().pstd_work_counts(self._need(), ctypes.byref(c), ctypes.byref(a), ctypes.byref(l_)))
+        return {"cells": c.value, "air_cells": a.value, "launches_per_step": l_.value}
