@@ -1,0 +1,327 @@
+"""Throughput of the GB300 PSTD solve (Gcell-steps/s).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload lshape|square]
+
+Workload (default ``lshape``): the multi-domain L-shaped scene -- 1200x600,
+600x600 and 600x1200 air cells (dx = 0.2 m) with a seeded mix of rigid and
+alpha = 0.3 + 50-cell-PML outer edges, 4 speakers, 16 receivers (seeded
+synthetic scene; the reference publishes no scenes).  A step is one full PSTD
+time step (6 RK stages) of the whole scene; the unit of work is one pressure
+cell of a non-rigid domain advanced one step.
+
+* ``value``: device-resident throughput, the K timed steps launched with
+  ``pstd_advance`` on a CUDA stream and timed with CUDA events on it.
+* ``e2e``: the same metric through the reference-facing API --
+  ``PSTDKernel.initialize_kernel`` (scene upload) + ``PSTDKernel.run`` with
+  every frame of p0 and every receiver sample delivered to host callbacks
+  (SaveNth = 1), host<->device copies included.
+* ``roofline``: the strip-pass kernel (pass_kernel<L>), 48 algorithmic bytes
+  per cell and RK stage (read px,py,vx,vy + the stage-start px,py,vx,vy, write
+  px,py,vx,vy), over its CUDA-event time measured in a second timed region
+  with events around every pass launch.
+* ``cpu_baseline``: the CPU restatement of the reference solver (oracle/),
+  OpenMP over all host cores, on a bounded sample of the same scene.
+
+``--impl reference`` times the reference's CPU algorithm (the oracle port; the
+reference itself cannot be built: Eigen, FFTW3f, Boost and Qt5 are absent) on
+the same scene with all host threads; under torchrun only rank 0 runs it.
+Multi-GPU runs are replicas: every rank solves its own scene (seed = rank),
+no collective on the data path; value = all ranks' cells x steps / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+L2_BYTES = 126 * 1024 * 1024
+BYTES_PER_CELL_STAGE = 48
+METRIC = "Gcell-steps/s"
+
+
+def workload(name: str, seed: int):
+    from openpstd_gb300 import scenes
+    if name == "lshape":
+        return scenes.l_shape(seed, steps=4000), ("L-shape 1200x600+600x600+600x1200 cells, dx 0.2 m, mixed rigid / "
+                                                  "alpha 0.3 + 50-cell PML edges, 4 speakers, 16 receivers")
+    if name == "square":
+        return scenes.plain_square(seed), "square 200x200 cells + 50-cell PML, 1 speaker, 4 receivers"
+    raise SystemExit(f"unknown workload {name}")
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, None
+    import torch.distributed as dist
+    rank = int(os.environ.get("RANK", "0"))
+    backend = "nccl"
+    dist.init_process_group(backend=backend)
+    return rank, ws, dist
+
+
+class ClockSampler:
+    """nvidia-smi samples (200 ms) over the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            for line in open(self.path):
+                p = [x.strip() for x in line.split(",")]
+                if len(p) >= 9 and p[1].replace(".", "").isdigit():
+                    rows.append(p)
+        finally:
+            os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no nvidia-smi samples"]}
+        sm = [float(r[1]) for r in rows]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": float(rows[0][2]), "reasons": reasons,
+                "samples": len(rows), "power_w_max": max(float(r[3]) for r in rows if r[3].replace(".", "").isdigit())}
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_per_cell_stage():
+    """DRAM bytes per cell and RK stage of the pass kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "pass_kernel_traffic.json")
+    if not os.path.exists(path):
+        return None, None
+    d = json.load(open(path))
+    return d.get("dram_bytes_per_cell_stage"), d.get("case")
+
+
+def cpu_rate(conf, seconds: float, threads: int):
+    """Gcell-steps/s of the oracle port on a bounded sample (whole steps, >= 1)."""
+    from oracle import oracle
+    oracle.build()
+    s = oracle.OracleScene(conf, 32)
+    cells = sum(s.domain_info(i)["size"][0] * s.domain_info(i)["size"][1]
+                for i in range(s.n_domains) if not s.domain_info(i)["is_rigid"])
+    s.run(1, threads=threads)   # warm-up (plans, caches)
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        s.run(1, threads=threads)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= seconds:
+            break
+    return cells * steps / el / 1e9, steps, el, cells
+
+
+def run_reference(args):
+    rank, ws, dist = dist_setup()
+    if rank != 0:
+        return
+    from oracle import oracle
+    conf, desc = workload(args.workload, 0)
+    threads = os.cpu_count() or 1
+    # W warm-up steps are folded into one untimed step; K steps are timed,
+    # capped at ~90 s of host time (the rate is per step, so the cap only
+    # bounds the sample)
+    oracle.build()
+    s = oracle.OracleScene(conf, 32)
+    cells = sum(s.domain_info(i)["size"][0] * s.domain_info(i)["size"][1]
+                for i in range(s.n_domains) if not s.domain_info(i)["is_rigid"])
+    for _ in range(min(args.warmup, 1)):
+        s.run(1, threads=threads)
+    done, t0 = 0, time.perf_counter()
+    while done < args.steps:
+        s.run(1, threads=threads)
+        done += 1
+        if time.perf_counter() - t0 > 90:
+            break
+    el = time.perf_counter() - t0
+    v = cells * done / el / 1e9
+    line = {"metric": METRIC, "value": v, "unit": METRIC, "n_gpus": ws, "steps": done, "warmup": args.warmup,
+            "ms_per_step": el * 1e3 / done, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded scene)", "impl": "reference",
+            "config": {"workload": desc, "cells_per_step": cells, "steps_requested": args.steps},
+            "cpu_baseline": {"value": v, "unit": METRIC, "cores": threads, "kind": "port",
+                             "sample": f"{done} time steps of the workload (capped at 90 s)"},
+            "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import ctypes
+    import numpy as np
+    import torch
+    rank, ws, dist = dist_setup()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    from openpstd_gb300 import build as _b
+    _b.build()
+    from openpstd_gb300 import kernel
+    conf, desc = workload(args.workload, rank)
+    k = kernel.PSTDKernel()
+    k.initialize_kernel(conf)
+    wc = k.work_counts()
+    cells = wc["cells"]
+    stream = torch.cuda.Stream()
+    sh = stream.cuda_stream
+
+    def barrier():
+        if dist:
+            dist.barrier()
+
+    # ---- device-resident timed region
+    k.advance(args.warmup, sh)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        k.advance(args.steps, sh)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    ms = e0.elapsed_time(e1)
+    clocks = clk.summary()
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        c = torch.tensor([float(cells)], device="cuda")
+        dist.all_reduce(c)
+        total_cells = float(c.item())
+    else:
+        total_cells = float(cells)
+    value = total_cells * args.steps / (ms / 1e3) / 1e9
+
+    # ---- pass-kernel timing (events around every pass launch)
+    prof_steps = max(3, min(args.steps, 200))
+    torch.cuda.synchronize()
+    prof = k.profile_passes(prof_steps, sh)
+    stage_ms = prof["ms_stage"]
+    launches = prof["stage_launches"]
+    alg_bytes = cells * BYTES_PER_CELL_STAGE * 6 * prof_steps
+    peak, peak_kind = peaks()
+    achieved = alg_bytes / (stage_ms / 1e3) / 1e9
+    tpcs, tcase = traffic_per_cell_stage()
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": (tpcs * cells * 6 * prof_steps / launches) if tpcs else None,
+                "kernel": "stage_kernel<L,...> (all strip-length buckets of an RK stage)",
+                "algorithmic_bytes_per_launch": alg_bytes / launches, "launches": launches,
+                "avg_launch_us": stage_ms * 1e3 / launches, "peak_source": f"{peak_kind} hbm_gbs",
+                "traffic_source": tcase, "stage_share_of_step": stage_ms / prof["ms_total"],
+                "plan": k.plan_info().strip().splitlines()}
+
+    # ---- end-to-end through the reference-facing API (host callbacks)
+    e2e_steps = min(args.steps, 400)
+    ce = conf.copy()
+    dt = ce.Settings.GetTimeStep()
+    ce.Settings.SetRenderTime(float(np.float32((e2e_steps + 0.5) * float(dt))))
+    assert ce.Settings.framecount() == e2e_steps
+    sizes = {"frame_bytes": 0, "sample_bytes": 0}
+
+    class Sink(kernel.KernelCallback):
+        def WriteFrame(self, frame, domain, data):
+            sizes["frame_bytes"] += data.nbytes
+
+        def WriteSample(self, start, receiver, data):
+            sizes["sample_bytes"] += 4 * len(data)
+
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ke = kernel.PSTDKernel()
+    ke.initialize_kernel(ce)
+    ke.run(Sink())
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    cfg_bytes = sum(ctypes.sizeof(x) for x in (ke._cc.c,)) + 40 * len(ce.Domains) + 12 * (len(ce.Speakers) + len(ce.Receivers))
+    ke.close()
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": total_cells * e2e_steps / e2e_s / 1e9, "unit": METRIC,
+           "h2d_bytes_per_step": cfg_bytes / e2e_steps,
+           "d2h_bytes_per_step": (sizes["frame_bytes"] + sizes["sample_bytes"]) / e2e_steps,
+           "steps": e2e_steps, "path": "PSTDKernel.initialize_kernel + run(WriteFrame every frame, WriteSample)"}
+
+    if rank != 0:
+        return
+    state_bytes = 3 * 4 * cells * 5
+    line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene, no published scene exists)",
+            "config": {"workload": desc, "cells_per_step_per_gpu": cells, "air_cells": wc["air_cells"],
+                       "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
+                       "l2": f"no flush: resident state {state_bytes / 2**20:.0f} MiB (3 sets x 5 fields) > L2",
+                       "cuda_graphs": "one graph per time step (3-phase set rotation)"},
+            "roofline": roofline, "e2e": e2e, "clocks": clocks,
+            "gpu_launches": wc["launches_per_step"] * args.steps}
+    if ws == 1 and not args.no_cpu_baseline:
+        v, steps, el, ccells = cpu_rate(conf, args.cpu_seconds, os.cpu_count() or 1)
+        line["cpu_baseline"] = {"value": v, "unit": METRIC, "cores": os.cpu_count() or 1, "kind": "port",
+                                "sample": f"{steps} time steps of the same scene in {el:.1f} s (oracle, OpenMP)"}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", default="lshape")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -177,6 +177,13 @@ typedef struct pstd_domain_info {
     float alpha, impedance, rho;
 } pstd_domain_info;
 
+/* Build only the host-side scene (no device state, no GPU needed) so that
+ * the scene can be inspected; device calls on such a handle return
+ * PSTD_ERR_NOT_CONFIGURED.  Release with pstd_destroy. */
+int pstd_scene_build(const pstd_config* config, pstd_kernel** out);
+/* Strip plan of a domain: number of interface runs along axis (0 x, 1 y) and
+ * for each run (first strip, count, low neighbour, high neighbour); -1 = none. */
+int pstd_scene_strip_runs(pstd_kernel* k, int32_t index, int32_t axis, int32_t* runs, int32_t cap, int32_t* n);
 int pstd_scene_domain_count(pstd_kernel* k, int32_t* n);
 int pstd_scene_domain_info(pstd_kernel* k, int32_t index, pstd_domain_info* out);
 /* dir: 0 LEFT 1 RIGHT 2 TOP 3 BOTTOM; writes scene indices of the neighbours */
@@ -185,12 +192,17 @@ int pstd_scene_neighbours(pstd_kernel* k, int32_t index, int32_t dir, int32_t* o
  * (1 where the domain is not attenuated along that axis). */
 int pstd_scene_attenuation(pstd_kernel* k, int32_t index, float* ax_p, float* ax_v, float* ay_p, float* ay_v);
 
-/* ---- timing of the strip-derivative passes (no reference counterpart) --- */
-/* Advance n_steps with CUDA events around every pass launch; returns the summed
- * device time [ms] of the x-direction and y-direction passes and the number of
- * launches of each.  Results are identical to pstd_advance. */
+/* ---- timing of the stage kernels (no reference counterpart) ------------ */
+/* Advance n_steps with CUDA events around every RK stage (its strip-length
+ * buckets launched back to back); returns the summed device time [ms] of the
+ * stage-kernel launches, the time of the whole region, and the launch counts.
+ * Results are identical to pstd_advance. */
 int pstd_profile_passes(pstd_kernel* k, int32_t n_steps, void* stream,
-                        float* ms_x, float* ms_y, int32_t* launches_x, int32_t* launches_y);
+                        float* ms_stage, float* ms_total, int32_t* stage_launches, int32_t* total_launches);
+
+/* Stage-kernel plan: one line per strip-length bucket (length, jobs,
+ * variant chosen by the autotuner and the timings it compared). */
+int pstd_plan_info(pstd_kernel* k, char* buf, int32_t cap);
 
 /* Counts that define the work: cells advanced per step (pressure cells of
  * non-rigid domains), of which air cells, and the number of kernel launches

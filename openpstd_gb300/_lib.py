@@ -52,11 +52,14 @@ SIGNATURES = {
     "pstd_steps_done": (ctypes.c_int, [_vp, _P(_i32)]),
     "pstd_get_receivers": (ctypes.c_int, [_vp, _i32, _i32, _P(_f32)]),
     "pstd_snapshot": (ctypes.c_int, [_vp, _i32, _i32, _P(_f32), _i64]),
+    "pstd_scene_build": (ctypes.c_int, [_P(c_config), _P(_vp)]),
+    "pstd_scene_strip_runs": (ctypes.c_int, [_vp, _i32, _i32, _P(_i32), _i32, _P(_i32)]),
     "pstd_scene_domain_count": (ctypes.c_int, [_vp, _P(_i32)]),
     "pstd_scene_domain_info": (ctypes.c_int, [_vp, _i32, _P(c_domain_info)]),
     "pstd_scene_neighbours": (ctypes.c_int, [_vp, _i32, _i32, _P(_i32), _i32, _P(_i32)]),
     "pstd_scene_attenuation": (ctypes.c_int, [_vp, _i32, _P(_f32), _P(_f32), _P(_f32), _P(_f32)]),
     "pstd_profile_passes": (ctypes.c_int, [_vp, _i32, _vp, _P(_f32), _P(_f32), _P(_i32), _P(_i32)]),
+    "pstd_plan_info": (ctypes.c_int, [_vp, ctypes.c_char_p, _i32]),
     "pstd_work_counts": (ctypes.c_int, [_vp, _P(_i64), _P(_i64), _P(_i32)]),
     "pstd_last_error": (ctypes.c_char_p, []),
     "pstd_version": (ctypes.c_char_p, []),

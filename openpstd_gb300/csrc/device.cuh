@@ -1,14 +1,25 @@
 // device.cuh -- data layout shared by the host plan and the sm_103a kernels.
 //
-// Field storage: three state sets (A, B, C) of identical layout.  Every domain
-// owns five row-major arrays in each set, rows padded to a multiple of 32
-// floats (128 B):
-//   p0, px, py : Ny rows x Nx      (pitch_p)
-//   vx         : Ny rows x (Nx+1)  (pitch_vx)
-//   vy         : (Ny+1) rows x Nx  (pitch_vy)
+// Field storage.  Three rotating state sets (A, B, C) of identical layout hold
+// px, py, vx, vy of every non-rigid domain; rows are padded to a multiple of
+// 32 floats (128 B):
+//   px, py : Ny rows x Nx      (pitch_p)
+//   vx     : Ny rows x (Nx+1)  (pitch_vx)
+//   vy     : (Ny+1) rows x Nx  (pitch_vy)
 // A time step reads the stage-start set P and writes the six RK stages
 // alternately into the two other sets; the last stage's set becomes P of the
-// next step, so no push_values copy is made (kernel/Solver.cpp:73-76 copies).
+// next step, so there is no push_values copy (kernel/Solver.cpp:73-76).
+//
+// p0 is not stored per stage: every stage forms p0 = px + py of the previous
+// stage while loading (kernel/Solver.cpp:114-116 computes exactly that sum).
+// One p0 array per domain holds the values the reference reads at the first
+// stage of a step where they differ from px + py: the speaker initial p0 at
+// the very first step (kernel/core/Speaker.cpp:35) and, for PML domains, p0
+// from before the PML multiply (kernel/Solver.cpp:85 leaves p0 stale).
+//
+// Rigid domains are never RK-updated (kernel/Solver.cpp:101,110): their
+// fields live once in a fixed buffer that only the per-step PML kernel
+// touches.
 #pragma once
 #include <cstdint>
 
@@ -18,20 +29,23 @@ struct DevDomain {
     int nx, ny;
     int pitch_p, pitch_vx, pitch_vy;
     int att_xp, att_xv, att_yp, att_yv;   // offsets into the attenuation table, -1 = none
-    int pml;
-    long long o_p0, o_px, o_py, o_vx, o_vy;   // float offsets inside a state set
-    float rho;       // domain density (float, as the reference)
-    float c2;        // c1*c1 (float)
-    float cdt[6];    // dt * rk_coefficient[k] (float)
+    int pml;                              // PML domain (stale p0 at the first stage of a step)
+    int fixed;                            // rigid: fields in the fixed buffer
+    long long o_px, o_py, o_vx, o_vy;     // float offsets inside a state set (or the fixed buffer)
+    long long o_p0;                       // float offset in the p0 array
+    float rho;                            // domain density (float, as the reference)
+    float c2;                             // c1*c1 (float)
+    float cdt[6];                         // dt * rk_coefficient[k] (float)
 };
 
 enum JobKind : int {
-    JK_VEL = 1,   // derivative of the velocity strip (updates px / py); else of p0 (updates vx / vy)
-    JK_Y = 2,     // y-direction strips (columns); else x-direction (rows)
+    JK_VEL = 1,    // derivative of the velocity strip (updates px / py); else of p0 (updates vx / vy)
+    JK_Y = 2,      // y-direction strips (columns); else x-direction (rows)
+    JK_COPY = 4,   // axis not updated (should_update == false): carry the axis' fields through
 };
 
-// A batch of at most 2*CS adjacent strips of one domain that share the same
-// interface neighbours; one CTA per job.
+// Up to 2*CS adjacent strips of one domain that share both interface
+// neighbours; one CTA per job.
 struct DevJob {
     int dom, first, count, kind;
     int W;            // window length (after halving)
@@ -40,12 +54,6 @@ struct DevJob {
     float R1, T1, R2, T2;   // reflection / transmission of the two bands
     int dtab;         // float2 offset of the permuted derivative filter
     int wtab;         // float offset of the 2W+1 window coefficients
-};
-
-// A domain whose fields are only carried through one pass (rigid domain or
-// should_update == false along that axis).
-struct DevCopy {
-    int dom, kind;    // kind: JK_Y or 0
 };
 
 struct DevReceiver {

@@ -1,4 +1,5 @@
-// launch.hpp -- host launchers of the kernels in kernels.cu.
+// launch.hpp -- host-side view of the kernels: stage-kernel variants and the
+// small per-step kernels.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -6,32 +7,43 @@
 
 namespace pstd {
 
-struct PassArgs {
+struct StageArgs {
     const DevJob* jobs;
     const DevDomain* doms;
-    const float* in;      // state of the previous stage (derivative input)
-    const float* prev;    // stage-start state
-    float* out;           // new state
-    const float2* filt;   // derivative filters (position order)
-    const float* win;     // window coefficients
-    const float2* tw;     // twiddles exp(-2 pi i j / L), j < L
-    const float* att;     // PML attenuation profiles
-    int stage;            // 0..5
-    int last;             // 1 at the sixth stage
+    const float* in;        // state after the previous stage (derivative input)
+    const float* prev;      // stage-start state
+    float* out;             // new state
+    const float* fixed;     // fields of rigid domains
+    const float* p0;        // per-domain p0 read at the first stage (initial / stale)
+    const int* first_step;  // 1 while the very first step runs
+    const float2* filt;     // derivative filters (position order)
+    const float* win;       // window coefficients
+    const float2* tw;       // twiddles exp(-2 pi i j / L), j < L
+    const float* att;       // PML attenuation profiles
+    int stage;              // 0..5
+    int last;               // 1 at the sixth stage
 };
 
-// strips per CTA for transform length L (0 if L is not supported)
-int pass_strips_per_job(int L);
-// radix sequence of the in-place transform of length L
-void pass_radices(int L, int* r, int* np);
-// allow the pass kernels their dynamic shared memory (call before capture)
-cudaError_t prepare_pass_kernels();
-cudaError_t launch_pass(int L, int n_jobs, const PassArgs& a, cudaStream_t st);
-cudaError_t launch_copy(const DevCopy* copies, int n, const DevDomain* doms, const float* prev, float* out,
-                        const float* att, int last, cudaStream_t st);
+// One compiled shape of the stage kernel for one transform length.
+struct StageVariant {
+    int L, CS, NT, smem, np;
+    int r[4];                                                   // radix of each pass
+    cudaError_t (*launch)(int n_jobs, const StageArgs& a, cudaStream_t st);
+    cudaError_t (*prepare)();
+    const char* name;
+};
+
+// all variants compiled for length L (nullptr / 0 if L is not supported)
+int stage_variants(int L, const StageVariant** out);
+
+cudaError_t launch_pml_post(const int* doms_idx, int n, const DevDomain* doms, float* set, float* fixed, float* p0,
+                            const float* att, int* first_step, cudaStream_t st);
 cudaError_t launch_speakers(const DevDomain* doms, const int* x0, const int* y0, int n_dom, const DevSpeaker* spk,
-                            int n_spk, float dx, float bw, float* set, cudaStream_t st);
+                            int n_spk, float dx, float bw, float* set, float* fixed, float* p0, cudaStream_t st);
 cudaError_t launch_receivers(const DevReceiver* rec, int n_rec, const DevDomain* doms, const float* set, float* ring,
                              int cap, int* counter, cudaStream_t st);
+// dense p0 = px + py of the given domains into dst (frames)
+cudaError_t launch_frame(const int* doms_idx, const long long* dst_off, int n, const DevDomain* doms, const float* set,
+                         float* dst, cudaStream_t st);
 
 }  // namespace pstd

@@ -1,0 +1,147 @@
+// misc.cu -- per-step kernels around the stage kernels, and the variant
+// registry.
+#include <cuda_runtime.h>
+
+#include "launch.hpp"
+
+namespace pstd {
+
+const StageVariant* stage_variants_small(int L, int* n);
+const StageVariant* stage_variants_mid(int L, int* n);
+const StageVariant* stage_variants_large(int L, int* n);
+const StageVariant* stage_variants_huge(int L, int* n);
+
+int stage_variants(int L, const StageVariant** out) {
+    int n = 0;
+    const StageVariant* v = nullptr;
+    if (L <= 256) v = stage_variants_small(L, &n);
+    else if (L <= 1024) v = stage_variants_mid(L, &n);
+    else if (L <= 2048) v = stage_variants_large(L, &n);
+    else v = stage_variants_huge(L, &n);
+    *out = v;
+    return v ? n : 0;
+}
+
+// After the sixth stage, for every PML domain (kernel/Solver.cpp:85,
+// kernel/core/Domain.cpp:716-725): keep p0 = px + py from before the multiply
+// (the reference does not recompute p0 after it), then px *= ax, py *= ay.
+// vx and vy of non-rigid domains were attenuated in the stage epilogue; rigid
+// domains (fields in the fixed buffer) get all four multiplies here.  Clears
+// the first-step flag.
+__global__ void pml_post_kernel(const int* idx, const DevDomain* doms, float* set, float* fixed, float* p0,
+                                const float* __restrict__ att, int* first_step) {
+    const DevDomain d = doms[idx[blockIdx.y]];
+    float* base = d.fixed ? fixed : set;
+    const int stride = gridDim.x * blockDim.x;
+    const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+    for (int k = t0; k < d.nx * d.ny; k += stride) {
+        const int r = k / d.nx, i = k - r * d.nx;
+        const long long e = (long long)r * d.pitch_p + i;
+        const float px = base[d.o_px + e], py = base[d.o_py + e];
+        p0[d.o_p0 + e] = __fadd_rn(px, py);
+        if (d.att_xp >= 0) base[d.o_px + e] = __fmul_rn(px, att[d.att_xp + i]);
+        if (d.att_yp >= 0) base[d.o_py + e] = __fmul_rn(py, att[d.att_yp + r]);
+    }
+    if (d.fixed) {
+        for (int k = t0; k < d.ny * (d.nx + 1); k += stride) {
+            const int r = k / (d.nx + 1), i = k - r * (d.nx + 1);
+            const long long e = d.o_vx + (long long)r * d.pitch_vx + i;
+            if (d.att_xv >= 0) base[e] = __fmul_rn(base[e], att[d.att_xv + i]);
+        }
+        for (int k = t0; k < (d.ny + 1) * d.nx; k += stride) {
+            const int r = k / d.nx, i = k - r * d.nx;
+            const long long e = d.o_vy + (long long)r * d.pitch_vy + i;
+            if (d.att_yv >= 0) base[e] = __fmul_rn(base[e], att[d.att_yv + r]);
+        }
+    }
+    if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) *first_step = 0;
+}
+
+// Gaussian speaker initial condition (kernel/core/Speaker.cpp:21-39) on every
+// domain, PML included; speakers are added in order.  Writes the initial p0
+// array and px, py of the initial set (rigid domains: of the fixed buffer).
+__global__ void speaker_kernel(const DevDomain* doms, const int* dom_x0, const int* dom_y0, const DevSpeaker* spk,
+                               int n_spk, float dx, float band_width, float* set, float* fixed, float* p0out) {
+    const DevDomain d = doms[blockIdx.y];
+    const float x0 = (float)dom_x0[blockIdx.y], y0 = (float)dom_y0[blockIdx.y];
+    float* base = d.fixed ? fixed : set;
+    const int stride = gridDim.x * blockDim.x;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < d.nx * d.ny; k += stride) {
+        const int j = k / d.nx, i = k - j * d.nx;   // j: row (y), i: column (x)
+        float p0 = 0.f, px = 0.f, py = 0.f;
+        for (int s = 0; s < n_spk; s++) {
+            const float rx = __fsub_rn(spk[s].x, x0), ry = __fsub_rn(spk[s].y, y0);
+            const float ax = __fsub_rn(rx, (float)i), ay = __fsub_rn(ry, (float)j);
+            // SQR(a*dx) expands to a*dx*a*dx in the reference
+            const float sq = __fadd_rn(__fmul_rn(__fmul_rn(__fmul_rn(ax, dx), ax), dx),
+                                       __fmul_rn(__fmul_rn(__fmul_rn(ay, dx), ay), dx));
+            const float p = expf(__fmul_rn(-band_width, sq));
+            const float ang = atan2f(ax, ay);
+            const float c = cosf(ang), sn = sinf(ang);
+            p0 = __fadd_rn(p0, p);
+            px = __fadd_rn(px, __fmul_rn(__fmul_rn(c, c), p));
+            py = __fadd_rn(py, __fmul_rn(__fmul_rn(sn, sn), p));
+        }
+        const long long e = (long long)j * d.pitch_p + i;
+        p0out[d.o_p0 + e] = p0;
+        base[d.o_px + e] = px;
+        base[d.o_py + e] = py;
+    }
+}
+
+// One sample per receiver after the step (kernel/core/Receiver.cpp:80-83):
+// p0(rel.x, rel.y) of the (non-PML) container, i.e. row rel.x, column rel.y,
+// where p0 = px + py of the last stage.
+__global__ void receiver_kernel(const DevReceiver* rec, int n_rec, const DevDomain* doms, const float* __restrict__ set,
+                                float* ring, int ring_cap, int* counter) {
+    const int step = *counter;
+    for (int r = threadIdx.x; r < n_rec; r += blockDim.x) {
+        const DevReceiver q = rec[r];
+        const DevDomain d = doms[q.dom];
+        const long long e = (long long)q.row * d.pitch_p + q.col;
+        ring[(long long)(step % ring_cap) * n_rec + r] = __fadd_rn(set[d.o_px + e], set[d.o_py + e]);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) *counter = step + 1;
+}
+
+__global__ void frame_kernel(const int* idx, const long long* dst_off, const DevDomain* doms,
+                             const float* __restrict__ set, float* dst) {
+    const DevDomain d = doms[idx[blockIdx.y]];
+    float* out = dst + dst_off[blockIdx.y];
+    const int stride = gridDim.x * blockDim.x;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < d.nx * d.ny; k += stride) {
+        const int r = k / d.nx, i = k - r * d.nx;
+        const long long e = (long long)r * d.pitch_p + i;
+        out[k] = __fadd_rn(set[d.o_px + e], set[d.o_py + e]);
+    }
+}
+
+cudaError_t launch_pml_post(const int* idx, int n, const DevDomain* doms, float* set, float* fixed, float* p0,
+                            const float* att, int* first_step, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    pml_post_kernel<<<dim3(8, n), 256, 0, st>>>(idx, doms, set, fixed, p0, att, first_step);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_speakers(const DevDomain* doms, const int* x0, const int* y0, int n_dom, const DevSpeaker* spk,
+                            int n_spk, float dx, float bw, float* set, float* fixed, float* p0, cudaStream_t st) {
+    if (n_dom <= 0) return cudaSuccess;
+    speaker_kernel<<<dim3(64, n_dom), 256, 0, st>>>(doms, x0, y0, spk, n_spk, dx, bw, set, fixed, p0);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_receivers(const DevReceiver* rec, int n_rec, const DevDomain* doms, const float* set, float* ring,
+                             int cap, int* counter, cudaStream_t st) {
+    receiver_kernel<<<1, 256, 0, st>>>(rec, n_rec, doms, set, ring, cap, counter);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_frame(const int* idx, const long long* dst_off, int n, const DevDomain* doms, const float* set,
+                         float* dst, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    frame_kernel<<<dim3(64, n), 256, 0, st>>>(idx, dst_off, doms, set, dst);
+    return cudaGetLastError();
+}
+
+}  // namespace pstd

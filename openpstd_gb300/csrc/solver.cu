@@ -4,20 +4,26 @@
 // pstd_create builds the scene on the host (scene.cpp), the FP64 tables
 // (window, derivative filters, twiddles, PML profiles), the device field
 // layout (device.cuh) and the strip-job plan, then uploads everything once.
-// A time step is 12 strip passes (x then y for each of the 6 RK stages,
-// kernel/Solver.cpp:77-79,95-117) plus one receiver gather; the three phases
-// of the state-set rotation are captured as three CUDA graphs.
+// A time step (kernel/Solver.cpp:71-117) is six RK stages; each stage is one
+// launch of the stage kernel per strip-length bucket, all buckets running
+// concurrently (they read only the previous stage); then one PML kernel and
+// one receiver gather.  The three phases of the state-set rotation are
+// captured as three CUDA graphs.  For every bucket the stage-kernel variant
+// (strips per CTA, threads, radix plan) is picked by timing each compiled
+// variant on the scene's own jobs at create time.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
 #include <complex>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <map>
 #include <memory>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "../../include/pstd_gb300.h"
@@ -49,7 +55,7 @@ struct DevBuf {
         if (count) CK(cudaMalloc(&p, count * sizeof(T)));
     }
     void upload(const std::vector<T>& v) {
-        alloc(v.size());
+        alloc(std::max<size_t>(v.size(), 1));
         if (!v.empty()) CK(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
     }
     void release() {
@@ -60,17 +66,24 @@ struct DevBuf {
     ~DevBuf() { release(); }
 };
 
-struct Group {     // one pass launch: jobs of one strip length
-    int L;
-    int offset, count;
+struct PinnedBuf {
+    float* p = nullptr;
+    size_t n = 0;
+    void alloc(size_t count) {
+        if (count <= n) return;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        n = 0;
+        CK(cudaMallocHost(&p, count * sizeof(float)));
+        n = count;
+    }
+    ~PinnedBuf() { if (p) cudaFreeHost(p); }
 };
 
-// position of spectrum bin k after the in-place decimation-in-frequency
+// Position of spectrum bin k after the in-place decimation-in-frequency
 // transform with radices r[0..np): k = k1 + r1 k2 + r1 r2 k3 + ... sits at
 // k1 (L/r1) + k2 (L/(r1 r2)) + ...
-static std::vector<int> bin_positions(int L) {
-    int r[4], np;
-    pass_radices(L, r, &np);
+static std::vector<int> bin_positions(int L, const int* r, int np) {
     std::vector<int> pos(L);
     for (int k = 0; k < L; k++) {
         int rem = k, span = L, p = 0;
@@ -85,36 +98,62 @@ static std::vector<int> bin_positions(int L) {
     return pos;
 }
 
+struct Bucket {
+    int L = 0;
+    const StageVariant* var = nullptr;
+    int off = 0, n = 0;            // jobs in djobs
+    int tw_off = 0;                // float2 offset of the twiddles in dtw
+    std::string choice;            // autotune record
+};
+
 struct Kernel {
     Scene sc;
     int device = 0;
     cudaStream_t stream = nullptr;
+    std::vector<cudaStream_t> side;     // one per bucket, for concurrent capture
     pstd_callbacks logcb{};
     bool have_logcb = false;
+    bool host_only = false;             // built by pstd_scene_build: no device state
+    bool autotune = true;
 
     // layout
     std::vector<DevDomain> hdoms;
-    size_t set_floats = 0;
-    DevBuf<float> sets[3];
-    DevBuf<float> init_set;
+    size_t set_floats = 0, fixed_floats = 0, p0_floats = 0;
+    DevBuf<float> sets[3], init_set, fixed, init_fixed, p0, init_p0;
+    DevBuf<int> first_step;
     int cur = 0;              // set holding the current (stage-start) state
     int steps = 0;            // steps taken since reset
     int framecount = 0;
 
     DevBuf<DevDomain> ddoms;
     DevBuf<DevJob> djobs;
-    DevBuf<DevCopy> dcopies;
     DevBuf<float2> dfilt, dtw;
     DevBuf<float> dwin, datt;
+    DevBuf<int> dpml;                 // indices of PML domains
+    int n_pml = 0;
     DevBuf<DevReceiver> drec;
     DevBuf<float> dring;
     DevBuf<int> dcounter;
-    std::map<int, int> tw_offset;   // L -> float2 offset in dtw
-    std::vector<Group> xgroups, ygroups;
-    int xcopy_off = 0, xcopy_n = 0, ycopy_off = 0, ycopy_n = 0;
+    std::vector<Bucket> buckets;
     int ring_cap = 1;
     int n_rec = 0;
     int64_t cells = 0, air_cells = 0;
+
+    // host-side tables
+    std::vector<float> win;
+    std::map<int, int> win_off;
+    std::vector<float2> filt;
+    std::map<std::tuple<int, int, int, int, int, int>, int> filt_off;   // (L, vel, radices)
+    std::vector<float2> tw;
+    std::map<std::tuple<int, int, int, int, int>, int> tw_off;   // (L, radices)
+
+    // frames
+    std::vector<int> frame_doms;
+    std::vector<long long> frame_off;
+    size_t frame_floats = 0;
+    DevBuf<int> dframe_doms;
+    DevBuf<long long> dframe_off;
+    DevBuf<float> dframe;
 
     cudaGraphExec_t graphs[3] = {nullptr, nullptr, nullptr};
     bool graphs_ok = false;
@@ -125,21 +164,159 @@ struct Kernel {
 
     ~Kernel() {
         for (auto& g : graphs) if (g) cudaGraphExecDestroy(g);
+        for (auto s : side) cudaStreamDestroy(s);
         if (stream) cudaStreamDestroy(stream);
     }
 
+    // ---------------------------------------------------------------- tables
+    int window_of(int W) {
+        auto it = win_off.find(W);
+        if (it != win_off.end()) return it->second;
+        int o = (int)win.size();
+        // kernel/core/kernel_functions.cpp:327-333 (patch error cast to int)
+        double walpha = ((int)sc.s.patcherror - 40) / 20.0 + 1;
+        for (int i = -W; i <= W; i++) {
+            double x = (double)i / W;
+            double x6 = x * x * x * x * x * x;
+            win.push_back((float)std::exp(-std::log(10.0) * walpha * x6));
+        }
+        win_off[W] = o;
+        return o;
+    }
+
+    int filter_of(int L, bool vel, const StageVariant* v) {
+        auto key = std::make_tuple(L, (int)vel, v->r[0], v->r[1], v->r[2], v->r[3]);
+        auto it = filt_off.find(key);
+        if (it != filt_off.end()) return it->second;
+        int o = (int)filt.size();
+        // kernel/core/WisdomCache.cpp:53-75: k_j = j (pi/dx)/(L/2) for bins
+        // 0..L/2, factor exp(-/+ i k dx/2) * i k; Hermitian extension; 1/L
+        const double dx = (double)sc.s.dx;
+        const double kmax = M_PI / dx;
+        std::vector<std::complex<double>> full(L);
+        for (int j = 0; j <= L / 2; j++) {
+            double k = kmax * j / (L / 2);
+            full[j] = std::exp(std::complex<double>(0, (vel ? 0.5 : -0.5) * k * dx)) * std::complex<double>(0, k);
+        }
+        full[0] = std::complex<double>(full[0].real(), 0);
+        full[L / 2] = std::complex<double>(full[L / 2].real(), 0);   // c2r ignores the Nyquist imaginary part
+        for (int j = 1; j < L / 2; j++) full[L - j] = std::conj(full[j]);
+        std::vector<int> pos = bin_positions(L, v->r, v->np);
+        std::vector<float2> perm(L);
+        for (int j = 0; j < L; j++) {
+            std::complex<double> c = full[j] / (double)L;
+            perm[pos[j]] = make_float2((float)c.real(), (float)c.imag());
+        }
+        filt.insert(filt.end(), perm.begin(), perm.end());
+        filt_off[key] = o;
+        return o;
+    }
+
+    // per-pass twiddle tables of a radix plan: pass p (block size M, radix R)
+    // holds [n1][k] = exp(-2 pi i n1 k / M) for n1 < M/R, k < R; the offset
+    // of every pass is a multiple of 2 float2 (16-byte loads)
+    int twiddles_of(const StageVariant* v) {
+        auto key = std::make_tuple(v->L, v->r[0], v->r[1], v->r[2], v->r[3]);
+        auto it = tw_off.find(key);
+        if (it != tw_off.end()) return it->second;
+        if (tw.size() & 1) tw.push_back(make_float2(0, 0));
+        int o = (int)tw.size();
+        int M = v->L;
+        for (int p = 0; p + 1 < v->np; p++) {
+            const int R = v->r[p], Q = M / R;
+            for (int n1 = 0; n1 < Q; n1++)
+                for (int k = 0; k < R; k++) {
+                    double a = -2.0 * M_PI * (double)n1 * k / M;
+                    tw.push_back(make_float2((float)std::cos(a), (float)std::sin(a)));
+                }
+            M = Q;
+        }
+        tw_off[key] = o;
+        return o;
+    }
+
+    int run_length(const StripRun& r) const {
+        int n = sc.doms[r.dom].len(r.axis);
+        return Scene::next_pow2(n + 2 * sc.window_for(n));
+    }
+
+    // all jobs of bucket L for variant v (+ copy jobs if `with_copies`)
+    std::vector<DevJob> make_jobs(int L, const StageVariant* v, bool with_copies) {
+        std::vector<DevJob> jobs;
+        const int per = 2 * v->CS;
+        for (const StripRun& r : sc.runs) {
+            if (run_length(r) != L) continue;
+            const Domain& d = sc.doms[r.dom];
+            int n = d.len(r.axis);
+            int W = sc.window_for(n);
+            int wo = window_of(W);
+            for (int vel = 0; vel < 2; vel++) {
+                // reflection / transmission of the bands (kernel/core/kernel_functions.cpp:37-64)
+                float rs = d.rho;
+                float r1 = r.d1 >= 0 ? sc.doms[r.d1].rho : rs;
+                float r2 = r.d2 >= 0 ? sc.doms[r.d2].rho : rs;
+                float zn1 = r1 / rs, izn1 = rs / r1, zn2 = r2 / rs, izn2 = rs / r2;
+                float rlw1 = (zn1 - 1) / (zn1 + 1), tlw1 = (2 * zn1) / (zn1 + 1), tlw2 = (2 * izn1) / (izn1 + 1);
+                float rrw1 = (zn2 - 1) / (zn2 + 1), trw1 = (2 * zn2) / (zn2 + 1), trw2 = (2 * izn2) / (izn2 + 1);
+                DevJob j;
+                std::memset(&j, 0, sizeof j);
+                j.dom = r.dom;
+                j.kind = (vel ? JK_VEL : 0) | (r.axis == AX_Y ? JK_Y : 0);
+                j.W = W;
+                j.d1 = r.d1;
+                j.d2 = r.d2;
+                if (vel) { j.R1 = -rlw1; j.T1 = tlw1; j.R2 = -rrw1; j.T2 = trw1; }
+                else     { j.R1 = rlw1;  j.T1 = tlw2; j.R2 = rrw1;  j.T2 = trw2; }
+                j.dtab = filter_of(L, vel, v);
+                j.wtab = wo;
+                int s = r.first, end = r.first + r.count;
+                int origin = d.lo(r.axis);
+                while (s < end) {
+                    int e = std::min(end, (s / per + 1) * per);   // cut at multiples of `per`
+                    j.first = s;
+                    j.count = e - s;
+                    j.o1 = r.d1 >= 0 ? origin + s - sc.doms[r.d1].lo(r.axis) : 0;
+                    j.o2 = r.d2 >= 0 ? origin + s - sc.doms[r.d2].lo(r.axis) : 0;
+                    jobs.push_back(j);
+                    s = e;
+                }
+            }
+        }
+        if (with_copies) {
+            for (size_t k = 0; k < sc.doms.size(); k++) {
+                const Domain& d = sc.doms[k];
+                if (d.rigid) continue;
+                for (int ax = 0; ax < 2; ax++) {
+                    if (d.update[ax]) continue;
+                    DevJob j;
+                    std::memset(&j, 0, sizeof j);
+                    j.dom = (int)k;
+                    j.kind = JK_COPY | (ax == AX_Y ? JK_Y : 0);
+                    j.d1 = j.d2 = -1;
+                    jobs.push_back(j);
+                }
+            }
+        }
+        return jobs;
+    }
+
+    // ---------------------------------------------------------------- build
     void build(const pstd_config* cfg) {
         sc.build(cfg);
         framecount = sc.s.framecount();
+        if (const char* e = std::getenv("PSTD_AUTOTUNE")) autotune = std::atoi(e) != 0;
+        // PSTD_VARIANT=i pins every bucket to its i-th compiled variant (tests)
+        int forced = -1;
+        if (const char* e = std::getenv("PSTD_VARIANT")) { forced = std::atoi(e); autotune = false; }
         CK(cudaGetDevice(&device));
         CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
-        CK(prepare_pass_kernels());
 
         // ---- layout
         auto round32 = [](long long v) { return (v + 31) / 32 * 32; };
-        long long off = 0;
+        long long off = 0, foff = 0, poff = 0;
         hdoms.resize(sc.doms.size());
         std::vector<float> att;
+        std::vector<int> pml_idx;
         for (size_t k = 0; k < sc.doms.size(); k++) {
             const Domain& d = sc.doms[k];
             DevDomain& h = hdoms[k];
@@ -148,11 +325,13 @@ struct Kernel {
             h.pitch_p = (int)round32(d.nx);
             h.pitch_vx = (int)round32(d.nx + 1);
             h.pitch_vy = (int)round32(d.nx);
-            h.o_p0 = off; off = round32(off + (long long)h.pitch_p * d.ny);
-            h.o_px = off; off = round32(off + (long long)h.pitch_p * d.ny);
-            h.o_py = off; off = round32(off + (long long)h.pitch_p * d.ny);
-            h.o_vx = off; off = round32(off + (long long)h.pitch_vx * d.ny);
-            h.o_vy = off; off = round32(off + (long long)h.pitch_vy * (d.ny + 1));
+            h.fixed = d.rigid;
+            long long& o = d.rigid ? foff : off;
+            h.o_px = o; o = round32(o + (long long)h.pitch_p * d.ny);
+            h.o_py = o; o = round32(o + (long long)h.pitch_p * d.ny);
+            h.o_vx = o; o = round32(o + (long long)h.pitch_vx * d.ny);
+            h.o_vy = o; o = round32(o + (long long)h.pitch_vy * (d.ny + 1));
+            h.o_p0 = poff; poff = round32(poff + (long long)h.pitch_p * d.ny);
             h.rho = d.rho;
             h.c2 = sc.s.c1 * sc.s.c1;
             float dt = sc.s.dt();
@@ -160,6 +339,7 @@ struct Kernel {
             h.pml = d.pml;
             h.att_xp = h.att_xv = h.att_yp = h.att_yv = -1;
             if (d.pml) {
+                pml_idx.push_back((int)k);
                 std::vector<double> prof;
                 if (d.att_x) {
                     pml_profile(sc.s, false, d.asc_x, prof);
@@ -178,153 +358,46 @@ struct Kernel {
             if (!d.pml) air_cells += (int64_t)d.nx * d.ny;
         }
         set_floats = (size_t)std::max<long long>(off, 32);
+        fixed_floats = (size_t)std::max<long long>(foff, 32);
+        p0_floats = (size_t)std::max<long long>(poff, 32);
         if (att.empty()) att.push_back(1.f);
         datt.upload(att);
-
-        // ---- tables: windows, derivative filters, twiddles
-        std::map<int, int> win_off;            // W -> offset
-        std::vector<float> win;
-        std::map<std::pair<int, int>, int> filt_off;   // (L, velocity) -> offset
-        std::vector<float2> filt, tw;
-        auto window_of = [&](int W) {
-            auto it = win_off.find(W);
-            if (it != win_off.end()) return it->second;
-            int o = (int)win.size();
-            // kernel/core/kernel_functions.cpp:327-333, patch error cast to int
-            double walpha = ((int)sc.s.patcherror - 40) / 20.0 + 1;
-            for (int i = -W; i <= W; i++) {
-                double x = (double)i / W;
-                double x6 = x * x * x * x * x * x;
-                win.push_back((float)std::exp(-std::log(10.0) * walpha * x6));
-            }
-            win_off[W] = o;
-            return o;
-        };
-        auto filter_of = [&](int L, bool vel) {
-            auto key = std::make_pair(L, (int)vel);
-            auto it = filt_off.find(key);
-            if (it != filt_off.end()) return it->second;
-            int o = (int)filt.size();
-            // kernel/core/WisdomCache.cpp:53-75: k_j = j (pi/dx)/(L/2), factor
-            // exp(-/+ i k dx/2) * i k for bins 0..L/2, Hermitian extension, /L
-            const double dx = (double)sc.s.dx;
-            const double kmax = M_PI / dx;
-            std::vector<std::complex<double>> full(L);
-            for (int j = 0; j <= L / 2; j++) {
-                double k = kmax * j / (L / 2);
-                std::complex<double> ik(0, k);
-                std::complex<double> shift = std::exp(std::complex<double>(0, (vel ? 0.5 : -0.5) * k * dx));
-                full[j] = shift * ik;
-            }
-            full[0] = std::complex<double>(full[0].real(), 0);
-            full[L / 2] = std::complex<double>(full[L / 2].real(), 0);   // c2r ignores the Nyquist imaginary part
-            for (int j = 1; j < L / 2; j++) full[L - j] = std::conj(full[j]);
-            std::vector<int> pos = bin_positions(L);
-            std::vector<float2> perm(L);
-            for (int j = 0; j < L; j++) {
-                std::complex<double> v = full[j] / (double)L;
-                perm[pos[j]] = make_float2((float)v.real(), (float)v.imag());
-            }
-            filt.insert(filt.end(), perm.begin(), perm.end());
-            filt_off[key] = o;
-            return o;
-        };
-        auto twiddles_of = [&](int L) {
-            if (tw_offset.count(L)) return;
-            tw_offset[L] = (int)tw.size();
-            for (int j = 0; j < L; j++) {
-                double a = -2.0 * M_PI * j / L;
-                tw.push_back(make_float2((float)std::cos(a), (float)std::sin(a)));
-            }
-        };
-
-        // ---- jobs
-        std::map<int, std::vector<DevJob>> xj, yj;
-        for (const StripRun& r : sc.runs) {
-            const Domain& d = sc.doms[r.dom];
-            int n = d.len(r.axis);
-            int W = sc.window_for(n);
-            int L = Scene::next_pow2(n + 2 * W);
-            int per = pass_strips_per_job(L);
-            if (per <= 0)
-                throw SceneError(PSTD_ERR_UNSUPPORTED, "strip transform length " + std::to_string(L) + " is not supported (32..8192)");
-            twiddles_of(L);
-            int wo = window_of(W);
-            for (int vel = 0; vel < 2; vel++) {
-                int fo = filter_of(L, vel);
-                // reflection/transmission of the two bands (kernel/core/kernel_functions.cpp:37-64)
-                float rs = d.rho;
-                float r1 = r.d1 >= 0 ? sc.doms[r.d1].rho : rs;
-                float r2 = r.d2 >= 0 ? sc.doms[r.d2].rho : rs;
-                float zn1 = r1 / rs, izn1 = rs / r1, zn2 = r2 / rs, izn2 = rs / r2;
-                float rlw1 = (zn1 - 1) / (zn1 + 1), tlw1 = (2 * zn1) / (zn1 + 1), tlw2 = (2 * izn1) / (izn1 + 1);
-                float rrw1 = (zn2 - 1) / (zn2 + 1), trw1 = (2 * zn2) / (zn2 + 1), trw2 = (2 * izn2) / (izn2 + 1);
-                DevJob j;
-                std::memset(&j, 0, sizeof j);
-                j.dom = r.dom;
-                j.kind = (vel ? JK_VEL : 0) | (r.axis == AX_Y ? JK_Y : 0);
-                j.W = W;
-                j.d1 = r.d1; j.d2 = r.d2;
-                if (vel) { j.R1 = -rlw1; j.T1 = tlw1; j.R2 = -rrw1; j.T2 = trw1; }
-                else     { j.R1 = rlw1;  j.T1 = tlw2; j.R2 = rrw1;  j.T2 = trw2; }
-                j.dtab = fo;
-                j.wtab = wo;
-                // cut the run at multiples of `per` strips (relative to the domain)
-                int s = r.first, end = r.first + r.count;
-                while (s < end) {
-                    int e = std::min(end, (s / per + 1) * per);
-                    j.first = s;
-                    j.count = e - s;
-                    int origin = d.lo(r.axis);   // global strip coordinate of strip 0
-                    j.o1 = r.d1 >= 0 ? origin + s - sc.doms[r.d1].lo(r.axis) : 0;
-                    j.o2 = r.d2 >= 0 ? origin + s - sc.doms[r.d2].lo(r.axis) : 0;
-                    (r.axis == AX_X ? xj : yj)[L].push_back(j);
-                    s = e;
-                }
-            }
-        }
-        std::vector<DevJob> jobs;
-        for (auto* m : {&xj, &yj}) {
-            for (auto& kv : *m) {
-                Group g{kv.first, (int)jobs.size(), (int)kv.second.size()};
-                jobs.insert(jobs.end(), kv.second.begin(), kv.second.end());
-                (m == &xj ? xgroups : ygroups).push_back(g);
-            }
-        }
-        std::vector<DevCopy> copies;
-        for (size_t k = 0; k < sc.doms.size(); k++)
-            if (sc.doms[k].rigid || !sc.doms[k].update[AX_X]) copies.push_back({(int)k, 0});
-        xcopy_off = 0; xcopy_n = (int)copies.size();
-        for (size_t k = 0; k < sc.doms.size(); k++)
-            if (sc.doms[k].rigid || !sc.doms[k].update[AX_Y]) copies.push_back({(int)k, JK_Y});
-        ycopy_off = xcopy_n; ycopy_n = (int)copies.size() - xcopy_n;
-        if (jobs.empty()) jobs.push_back(DevJob{});
-        if (copies.empty()) copies.push_back(DevCopy{0, 0});
-        if (filt.empty()) filt.push_back(make_float2(0, 0));
-        if (tw.empty()) tw.push_back(make_float2(1, 0));
-        if (win.empty()) win.push_back(1.f);
-
+        n_pml = (int)pml_idx.size();
+        dpml.upload(pml_idx);
         ddoms.upload(hdoms);
-        djobs.upload(jobs);
-        dcopies.upload(copies);
-        dfilt.upload(filt);
-        dtw.upload(tw);
-        dwin.upload(win);
 
-        // ---- receivers
-        std::vector<DevReceiver> rec;
-        for (auto& r : sc.receivers) rec.push_back({r.dom, r.row, r.col});
-        n_rec = (int)rec.size();
-        if (rec.empty()) rec.push_back({0, 0, 0});
-        drec.upload(rec);
-        ring_cap = std::max(framecount, 1);
-        dring.alloc((size_t)ring_cap * std::max(n_rec, 1));
-        dcounter.alloc(1);
+        // ---- buckets
+        std::vector<int> Ls;
+        for (const StripRun& r : sc.runs) {
+            int L = run_length(r);
+            if (std::find(Ls.begin(), Ls.end(), L) == Ls.end()) Ls.push_back(L);
+        }
+        std::sort(Ls.begin(), Ls.end());
+        for (int L : Ls) {
+            const StageVariant* vs;
+            int nv = stage_variants(L, &vs);
+            if (nv <= 0)
+                throw SceneError(PSTD_ERR_UNSUPPORTED, "strip transform length " + std::to_string(L) +
+                                                           " is outside the compiled range 32..8192");
+            for (int i = 0; i < nv; i++) CK(vs[i].prepare());
+            Bucket b;
+            b.L = L;
+            b.var = &vs[forced >= 0 ? std::min(forced, nv - 1) : 0];
+            if (forced >= 0) b.choice = " pinned";
+            buckets.push_back(b);
+        }
 
-        // ---- fields: initial condition into init_set, then copy
+        // ---- fields: initial condition
         for (auto& s : sets) s.alloc(set_floats);
         init_set.alloc(set_floats);
+        fixed.alloc(fixed_floats);
+        init_fixed.alloc(fixed_floats);
+        p0.alloc(p0_floats);
+        init_p0.alloc(p0_floats);
+        first_step.alloc(1);
         CK(cudaMemsetAsync(init_set.p, 0, set_floats * sizeof(float), stream));
+        CK(cudaMemsetAsync(init_fixed.p, 0, fixed_floats * sizeof(float), stream));
+        CK(cudaMemsetAsync(init_p0.p, 0, p0_floats * sizeof(float), stream));
         if (!sc.speakers.empty()) {
             std::vector<int> x0, y0;
             for (auto& d : sc.doms) { x0.push_back(d.x0); y0.push_back(d.y0); }
@@ -336,84 +409,216 @@ struct Kernel {
             DevBuf<DevSpeaker> dspk;
             dspk.upload(spk);
             CK(launch_speakers(ddoms.p, dx0.p, dy0.p, (int)sc.doms.size(), dspk.p, (int)spk.size(), sc.s.dx,
-                               sc.s.band_width, init_set.p, stream));
+                               sc.s.band_width, init_set.p, init_fixed.p, init_p0.p, stream));
             CK(cudaStreamSynchronize(stream));
         }
+
+        // ---- receivers, frames
+        std::vector<DevReceiver> rec;
+        for (auto& r : sc.receivers) rec.push_back({r.dom, r.row, r.col});
+        n_rec = (int)rec.size();
+        drec.upload(rec);
+        ring_cap = std::max(framecount, 1);
+        dring.alloc((size_t)ring_cap * std::max(n_rec, 1));
+        dcounter.alloc(1);
+        frame_floats = 0;
+        for (size_t k = 0; k < sc.doms.size(); k++) {
+            if (sc.doms[k].pml) continue;
+            frame_doms.push_back((int)k);
+            frame_off.push_back((long long)frame_floats);
+            frame_floats += (size_t)sc.doms[k].nx * sc.doms[k].ny;
+        }
+        dframe_doms.upload(frame_doms);
+        dframe_off.upload(frame_off);
+        dframe.alloc(std::max<size_t>(frame_floats, 1));
+
+        // ---- tables and the job plan (autotuned)
         reset();
-        CK(cudaStreamSynchronize(stream));
+        plan(autotune);
+        reset();
+        for (size_t i = 0; i < buckets.size(); i++) {
+            cudaStream_t s;
+            CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+            side.push_back(s);
+        }
         capture_graphs();
+        std::string choice;
+        for (auto& b : buckets) choice += " [" + std::string(b.var->name) + b.choice + "]";
         log(PSTD_LOG_DEBUG, "scene: " + std::to_string(sc.doms.size()) + " domains, " + std::to_string(sc.speakers.size()) +
-                                " speakers, " + std::to_string(sc.receivers.size()) + " receivers");
+                                " speakers, " + std::to_string(sc.receivers.size()) + " receivers; stage kernels:" + choice);
+    }
+
+    StageArgs stage_args(int c, int k, const DevJob* jobs, const float2* twp) {
+        const int A = (c + 1) % 3, B = (c + 2) % 3;
+        StageArgs a;
+        a.jobs = jobs;
+        a.doms = ddoms.p;
+        a.in = sets[k == 0 ? c : ((k - 1) % 2 == 0 ? A : B)].p;
+        a.prev = sets[c].p;
+        a.out = sets[k % 2 == 0 ? A : B].p;
+        a.fixed = fixed.p;
+        a.p0 = p0.p;
+        a.first_step = first_step.p;
+        a.filt = dfilt.p;
+        a.win = dwin.p;
+        a.tw = twp;
+        a.att = datt.p;
+        a.stage = k;
+        a.last = k == 5;
+        return a;
+    }
+
+    void upload_tables() {
+        dfilt.upload(filt);
+        dtw.upload(tw);
+        dwin.upload(win);
+    }
+
+    // choose a variant per bucket by timing each on this scene's jobs
+    void plan(bool tune) {
+        if (tune) {
+            for (auto& b : buckets) {
+                const StageVariant* vs;
+                int nv = stage_variants(b.L, &vs);
+                if (nv <= 1) continue;
+                std::vector<std::vector<DevJob>> all(nv);
+                std::vector<int> twv(nv);
+                for (int i = 0; i < nv; i++) {
+                    all[i] = make_jobs(b.L, &vs[i], false);
+                    twv[i] = twiddles_of(&vs[i]);
+                }
+                upload_tables();
+                float best = 1e30f;
+                int best_i = 0;
+                std::string rec;
+                cudaEvent_t e0, e1;
+                CK(cudaEventCreate(&e0));
+                CK(cudaEventCreate(&e1));
+                for (int i = 0; i < nv; i++) {
+                    if (all[i].empty()) continue;
+                    DevBuf<DevJob> tj;
+                    tj.upload(all[i]);
+                    StageArgs a = stage_args(cur, 1, tj.p, dtw.p + twv[i]);
+                    for (int w = 0; w < 2; w++) CK(vs[i].launch((int)all[i].size(), a, stream));
+                    CK(cudaEventRecord(e0, stream));
+                    const int reps = 5;
+                    for (int w = 0; w < reps; w++) CK(vs[i].launch((int)all[i].size(), a, stream));
+                    CK(cudaEventRecord(e1, stream));
+                    CK(cudaEventSynchronize(e1));
+                    float ms;
+                    CK(cudaEventElapsedTime(&ms, e0, e1));
+                    ms /= reps;
+                    char buf[64];
+                    std::snprintf(buf, sizeof buf, " %d:%.1fus", i, ms * 1e3f);
+                    rec += buf;
+                    if (ms < best) { best = ms; best_i = i; }
+                }
+                cudaEventDestroy(e0);
+                cudaEventDestroy(e1);
+                b.var = &vs[best_i];
+                b.choice = " tuned" + rec;
+            }
+        }
+        std::vector<DevJob> jobs;
+        for (size_t i = 0; i < buckets.size(); i++) {
+            auto& b = buckets[i];
+            auto js = make_jobs(b.L, b.var, i + 1 == buckets.size());
+            b.tw_off = twiddles_of(b.var);
+            b.off = (int)jobs.size();
+            b.n = (int)js.size();
+            jobs.insert(jobs.end(), js.begin(), js.end());
+        }
+        upload_tables();
+        djobs.upload(jobs);
     }
 
     void reset() {
         for (auto& s : sets) CK(cudaMemsetAsync(s.p, 0, set_floats * sizeof(float), stream));
         CK(cudaMemcpyAsync(sets[0].p, init_set.p, set_floats * sizeof(float), cudaMemcpyDeviceToDevice, stream));
+        CK(cudaMemcpyAsync(fixed.p, init_fixed.p, fixed_floats * sizeof(float), cudaMemcpyDeviceToDevice, stream));
+        CK(cudaMemcpyAsync(p0.p, init_p0.p, p0_floats * sizeof(float), cudaMemcpyDeviceToDevice, stream));
+        const int one = 1;
+        CK(cudaMemcpyAsync(first_step.p, &one, sizeof(int), cudaMemcpyHostToDevice, stream));
         CK(cudaMemsetAsync(dcounter.p, 0, sizeof(int), stream));
+        CK(cudaStreamSynchronize(stream));
         cur = 0;
         steps = 0;
     }
 
-    int launches_per_step() const {
-        int per_stage = (int)xgroups.size() + (int)ygroups.size() + (xcopy_n > 0) + (ycopy_n > 0);
-        return 6 * per_stage + 1;
-    }
+    int launches_per_step() const { return 6 * (int)buckets.size() + (n_pml > 0) + 1; }
 
-    // enqueue one time step starting from set `c`; events (optional) bracket
-    // the x and y pass launches for timing
-    void enqueue_step(int c, cudaStream_t st, std::vector<std::pair<cudaEvent_t, cudaEvent_t>>* xev = nullptr,
-                      std::vector<std::pair<cudaEvent_t, cudaEvent_t>>* yev = nullptr) {
-        const int A = (c + 1) % 3, B = (c + 2) % 3;
+    // Enqueue one time step from set `c` on `st`.  concurrent: the buckets of
+    // a stage go on side streams (fork/join); ev (optional): events around
+    // each stage's launches, which then run back to back on `st`.
+    void enqueue_step(int c, cudaStream_t st, bool concurrent,
+                      std::vector<std::pair<cudaEvent_t, cudaEvent_t>>* ev = nullptr) {
+        const int B = (c + 2) % 3;
+        std::vector<cudaEvent_t> tmp;
+        auto mk = [&]() {
+            cudaEvent_t e;
+            CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+            tmp.push_back(e);
+            return e;
+        };
         for (int k = 0; k < 6; k++) {
-            const float* in = sets[k == 0 ? c : ((k - 1) % 2 == 0 ? A : B)].p;
-            float* out = sets[k % 2 == 0 ? A : B].p;
-            PassArgs a{nullptr, ddoms.p, in, sets[c].p, out, dfilt.p, dwin.p, nullptr, datt.p, k, k == 5};
-            for (int dir = 0; dir < 2; dir++) {
-                auto& groups = dir == 0 ? xgroups : ygroups;
-                auto* ev = dir == 0 ? xev : yev;
-                cudaEvent_t e0 = nullptr, e1 = nullptr;
-                if (ev) {
-                    CK(cudaEventCreate(&e0));
-                    CK(cudaEventCreate(&e1));
-                    CK(cudaEventRecord(e0, st));
+            cudaEvent_t t0 = nullptr, t1 = nullptr;
+            if (ev) {
+                CK(cudaEventCreate(&t0));
+                CK(cudaEventCreate(&t1));
+                CK(cudaEventRecord(t0, st));
+            }
+            if (concurrent && buckets.size() > 1) {
+                cudaEvent_t fork = mk();
+                CK(cudaEventRecord(fork, st));
+                std::vector<cudaEvent_t> joins;
+                for (size_t i = 0; i < buckets.size(); i++) {
+                    auto& b = buckets[i];
+                    cudaStream_t s = i == 0 ? st : side[i];
+                    if (i > 0) CK(cudaStreamWaitEvent(s, fork, 0));
+                    StageArgs a = stage_args(c, k, djobs.p + b.off, dtw.p + b.tw_off);
+                    CK(b.var->launch(b.n, a, s));
+                    if (i > 0) {
+                        cudaEvent_t j = mk();
+                        CK(cudaEventRecord(j, s));
+                        joins.push_back(j);
+                    }
                 }
-                for (const Group& g : groups) {
-                    a.jobs = djobs.p + g.offset;
-                    a.tw = dtw.p + tw_offset[g.L];
-                    CK(launch_pass(g.L, g.count, a, st));
+                for (auto j : joins) CK(cudaStreamWaitEvent(st, j, 0));
+            } else {
+                for (auto& b : buckets) {
+                    StageArgs a = stage_args(c, k, djobs.p + b.off, dtw.p + b.tw_off);
+                    CK(b.var->launch(b.n, a, st));
                 }
-                if (ev) {
-                    CK(cudaEventRecord(e1, st));
-                    ev->push_back({e0, e1});
-                }
-                int co = dir == 0 ? xcopy_off : ycopy_off, cn = dir == 0 ? xcopy_n : ycopy_n;
-                CK(launch_copy(dcopies.p + co, cn, ddoms.p, sets[c].p, out, datt.p, k == 5, st));
+            }
+            if (ev) {
+                CK(cudaEventRecord(t1, st));
+                ev->push_back({t0, t1});
             }
         }
+        if (n_pml > 0) CK(launch_pml_post(dpml.p, n_pml, ddoms.p, sets[B].p, fixed.p, p0.p, datt.p, first_step.p, st));
+        else CK(cudaMemsetAsync(first_step.p, 0, sizeof(int), st));
         CK(launch_receivers(drec.p, n_rec, ddoms.p, sets[B].p, dring.p, ring_cap, dcounter.p, st));
+        for (auto e : tmp) cudaEventDestroy(e);   // destruction is deferred until the event completes
     }
 
     void capture_graphs() {
         graphs_ok = false;
-        cudaStream_t cs;
-        CK(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
         bool ok = true;
         for (int c = 0; c < 3 && ok; c++) {
             cudaGraph_t g = nullptr;
-            if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess) { ok = false; break; }
+            if (cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) { ok = false; break; }
             try {
-                enqueue_step(c, cs);
+                enqueue_step(c, stream, true);
             } catch (...) {
-                cudaStreamEndCapture(cs, &g);
+                cudaStreamEndCapture(stream, &g);
                 if (g) cudaGraphDestroy(g);
                 ok = false;
                 break;
             }
-            if (cudaStreamEndCapture(cs, &g) != cudaSuccess || !g) { ok = false; break; }
+            if (cudaStreamEndCapture(stream, &g) != cudaSuccess || !g) { ok = false; break; }
             if (cudaGraphInstantiate(&graphs[c], g, 0) != cudaSuccess) { cudaGraphDestroy(g); ok = false; break; }
             cudaGraphDestroy(g);
         }
-        cudaStreamDestroy(cs);
         cudaGetLastError();
         graphs_ok = ok;
         if (!ok) log(PSTD_LOG_WARNING, "CUDA graph capture failed; launching kernels directly");
@@ -421,59 +626,35 @@ struct Kernel {
 
     void step(cudaStream_t st) {
         if (graphs_ok) CK(cudaGraphLaunch(graphs[cur], st));
-        else enqueue_step(cur, st);
+        else enqueue_step(cur, st, false);
         cur = (cur + 2) % 3;
         steps++;
     }
-
-    // p0 of a domain from the current set into a dense host buffer
-    void copy_p0(int k, float* dst, cudaStream_t st) {
-        const DevDomain& h = hdoms[k];
-        CK(cudaMemcpy2DAsync(dst, h.nx * sizeof(float), sets[cur].p + h.o_p0, h.pitch_p * sizeof(float),
-                             h.nx * sizeof(float), h.ny, cudaMemcpyDeviceToHost, st));
-    }
-};
-
-struct PinnedBuf {
-    float* p = nullptr;
-    size_t n = 0;
-    void alloc(size_t count) {
-        if (count <= n) return;
-        if (p) cudaFreeHost(p);
-        p = nullptr;
-        n = 0;
-        CK(cudaMallocHost(&p, count * sizeof(float)));
-        n = count;
-    }
-    ~PinnedBuf() { if (p) cudaFreeHost(p); }
 };
 
 static int run_frames(Kernel* k, const pstd_callbacks* cb) {
     const int nframes = k->framecount;
     const int save = std::max(1, k->sc.s.save_nth);
-    std::vector<int> emit_doms;
-    size_t frame_floats = 0;
-    for (size_t d = 0; d < k->sc.doms.size(); d++)
-        if (!k->sc.doms[d].pml) { emit_doms.push_back((int)d); frame_floats += (size_t)k->hdoms[d].nx * k->hdoms[d].ny; }
+    const size_t frame_floats = k->frame_floats;
     const int K = 3;   // frames in flight
     const size_t slot = frame_floats + (size_t)std::max(k->n_rec, 1);
     PinnedBuf stage;
     stage.alloc(slot * K);
     std::vector<cudaEvent_t> ev(K);
     for (auto& e : ev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-    struct Pending { int frame, slot, step; };
+    struct Pending { int frame, slot; };
     std::deque<Pending> q;
     int status = PSTD_OK;
     auto log = [&](int lvl, const std::string& m) { if (cb && cb->log) cb->log(cb->user, lvl, m.c_str()); };
     auto deliver = [&](const Pending& p) {
         CK(cudaEventSynchronize(ev[p.slot]));
         float* base = stage.p + slot * p.slot;
-        size_t o = 0;
-        for (int d : emit_doms) {
+        for (size_t i = 0; i < k->frame_doms.size(); i++) {
+            int d = k->frame_doms[i];
             size_t n = (size_t)k->hdoms[d].nx * k->hdoms[d].ny;
             if (cb && cb->write_frame && status == PSTD_OK)
-                if (cb->write_frame(cb->user, p.frame, k->sc.doms[d].id, base + o, (int64_t)n) != 0) status = PSTD_ERR_CALLBACK;
-            o += n;
+                if (cb->write_frame(cb->user, p.frame, k->sc.doms[d].id, base + k->frame_off[i], (int64_t)n) != 0)
+                    status = PSTD_ERR_CALLBACK;
         }
         for (int r = 0; r < k->n_rec; r++) {
             if (cb && cb->write_sample && status == PSTD_OK)
@@ -492,10 +673,10 @@ static int run_frames(Kernel* k, const pstd_callbacks* cb) {
             int s = next_slot;
             next_slot = (next_slot + 1) % K;
             float* base = stage.p + slot * s;
-            size_t o = 0;
-            for (int d : emit_doms) {
-                k->copy_p0(d, base + o, k->stream);
-                o += (size_t)k->hdoms[d].nx * k->hdoms[d].ny;
+            if (frame_floats) {
+                CK(launch_frame(k->dframe_doms.p, k->dframe_off.p, (int)k->frame_doms.size(), k->ddoms.p,
+                                k->sets[k->cur].p, k->dframe.p, k->stream));
+                CK(cudaMemcpyAsync(base, k->dframe.p, frame_floats * sizeof(float), cudaMemcpyDeviceToHost, k->stream));
             }
             if (k->n_rec > 0) {
                 int row = (k->steps - 1) % k->ring_cap;
@@ -503,7 +684,7 @@ static int run_frames(Kernel* k, const pstd_callbacks* cb) {
                                    cudaMemcpyDeviceToHost, k->stream));
             }
             CK(cudaEventRecord(ev[s], k->stream));
-            q.push_back({f, s, k->steps});
+            q.push_back({f, s});
         } else {
             log(PSTD_LOG_INFO, "Finished frame: " + std::to_string(f));
         }
@@ -548,11 +729,14 @@ static int fail(int code, const std::string& m) {
 
 #define NEED(h)                                                                                  \
     if (!(h) || !(h)->k) return fail(PSTD_ERR_NOT_CONFIGURED, "kernel handle is not configured");
+#define NEED_DEVICE(h)                                                                           \
+    NEED(h);                                                                                     \
+    if ((h)->k->host_only) return fail(PSTD_ERR_NOT_CONFIGURED, "handle holds a host-only scene");
 
 extern "C" {
 
 const char* pstd_last_error(void) { return g_error.c_str(); }
-const char* pstd_version(void) { return "pstd_gb300 0.1.0 (sm_103a)"; }
+const char* pstd_version(void) { return "pstd_gb300 0.2.0 (sm_103a)"; }
 
 int pstd_create(const pstd_config* config, const pstd_callbacks* log_cb, pstd_kernel** out) {
     if (!out) return fail(PSTD_ERR_INVALID, "out is NULL");
@@ -564,6 +748,20 @@ int pstd_create(const pstd_config* config, const pstd_callbacks* log_cb, pstd_ke
         h->k->log(PSTD_LOG_DEBUG, "Initializing kernel");
         h->k->build(config);
         h->k->log(PSTD_LOG_DEBUG, "Finished initializing kernel");
+        *out = h.release();
+        return PSTD_OK;
+    })
+}
+
+int pstd_scene_build(const pstd_config* config, pstd_kernel** out) {
+    if (!out) return fail(PSTD_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    GUARD({
+        auto h = std::make_unique<pstd_kernel>();
+        h->k = std::make_unique<Kernel>();
+        h->k->sc.build(config);
+        h->k->framecount = h->k->sc.s.framecount();
+        h->k->host_only = true;
         *out = h.release();
         return PSTD_OK;
     })
@@ -588,12 +786,12 @@ int pstd_get_metadata(pstd_kernel* h, int32_t* n_domains, int32_t* dims, int32_t
 }
 
 int pstd_run(pstd_kernel* h, const pstd_callbacks* cb) {
-    NEED(h);
+    NEED_DEVICE(h);
     GUARD({ return run_frames(h->k.get(), cb); })
 }
 
 int pstd_advance(pstd_kernel* h, int32_t n_steps, void* stream) {
-    NEED(h);
+    NEED_DEVICE(h);
     if (n_steps < 0) return fail(PSTD_ERR_INVALID, "negative step count");
     GUARD({
         cudaStream_t st = stream ? (cudaStream_t)stream : h->k->stream;
@@ -603,15 +801,16 @@ int pstd_advance(pstd_kernel* h, int32_t n_steps, void* stream) {
 }
 
 int pstd_reset(pstd_kernel* h) {
-    NEED(h);
+    NEED_DEVICE(h);
     GUARD({
+        CK(cudaDeviceSynchronize());
         h->k->reset();
         return PSTD_OK;
     })
 }
 
 int pstd_synchronize(pstd_kernel* h) {
-    NEED(h);
+    NEED_DEVICE(h);
     GUARD({
         CK(cudaStreamSynchronize(h->k->stream));
         CK(cudaDeviceSynchronize());
@@ -626,7 +825,7 @@ int pstd_steps_done(pstd_kernel* h, int32_t* steps) {
 }
 
 int pstd_get_receivers(pstd_kernel* h, int32_t first_step, int32_t n_steps, float* dst) {
-    NEED(h);
+    NEED_DEVICE(h);
     auto* k = h->k.get();
     if (first_step < 0 || n_steps < 0 || first_step + n_steps > k->steps || first_step < k->steps - k->ring_cap)
         return fail(PSTD_ERR_INVALID, "requested receiver steps are not in the device ring");
@@ -643,14 +842,15 @@ int pstd_get_receivers(pstd_kernel* h, int32_t first_step, int32_t n_steps, floa
 }
 
 int pstd_snapshot(pstd_kernel* h, int32_t idx, int32_t field, float* dst, int64_t n) {
-    NEED(h);
+    NEED_DEVICE(h);
     auto* k = h->k.get();
     if (idx < 0 || idx >= (int)k->hdoms.size()) return fail(PSTD_ERR_INVALID, "domain index out of range");
     const DevDomain& d = k->hdoms[idx];
+    const float* base = d.fixed ? k->fixed.p : k->sets[k->cur].p;
     int rows, cols, pitch;
     long long o;
     switch (field) {
-        case PSTD_FIELD_P0: rows = d.ny; cols = d.nx; pitch = d.pitch_p; o = d.o_p0; break;
+        case PSTD_FIELD_P0: rows = d.ny; cols = d.nx; pitch = d.pitch_p; o = d.o_px; break;
         case PSTD_FIELD_PX: rows = d.ny; cols = d.nx; pitch = d.pitch_p; o = d.o_px; break;
         case PSTD_FIELD_PY: rows = d.ny; cols = d.nx; pitch = d.pitch_p; o = d.o_py; break;
         case PSTD_FIELD_VX: rows = d.ny; cols = d.nx + 1; pitch = d.pitch_vx; o = d.o_vx; break;
@@ -660,10 +860,41 @@ int pstd_snapshot(pstd_kernel* h, int32_t idx, int32_t field, float* dst, int64_
     if (n != (int64_t)rows * cols) return fail(PSTD_ERR_INVALID, "destination size does not match the field");
     GUARD({
         CK(cudaDeviceSynchronize());
-        CK(cudaMemcpy2D(dst, cols * sizeof(float), k->sets[k->cur].p + o, pitch * sizeof(float), cols * sizeof(float),
-                        rows, cudaMemcpyDeviceToHost));
+        if (field == PSTD_FIELD_P0) {
+            // the reference's p0 after a step is px + py (kernel/Solver.cpp:114-116),
+            // except where it is stale (PML) or initial (no step taken yet)
+            if (d.pml || k->steps == 0) {
+                CK(cudaMemcpy2D(dst, cols * sizeof(float), k->p0.p + d.o_p0, pitch * sizeof(float), cols * sizeof(float),
+                                rows, cudaMemcpyDeviceToHost));
+            } else {
+                std::vector<float> a((size_t)rows * cols), b((size_t)rows * cols);
+                CK(cudaMemcpy2D(a.data(), cols * sizeof(float), base + d.o_px, pitch * sizeof(float), cols * sizeof(float),
+                                rows, cudaMemcpyDeviceToHost));
+                CK(cudaMemcpy2D(b.data(), cols * sizeof(float), base + d.o_py, pitch * sizeof(float), cols * sizeof(float),
+                                rows, cudaMemcpyDeviceToHost));
+                for (size_t i = 0; i < a.size(); i++) dst[i] = a[i] + b[i];
+            }
+        } else {
+            CK(cudaMemcpy2D(dst, cols * sizeof(float), base + o, pitch * sizeof(float), cols * sizeof(float), rows,
+                            cudaMemcpyDeviceToHost));
+        }
         return PSTD_OK;
     })
+}
+
+int pstd_scene_strip_runs(pstd_kernel* h, int32_t idx, int32_t axis, int32_t* runs, int32_t cap, int32_t* n) {
+    NEED(h);
+    auto& sc = h->k->sc;
+    int c = 0;
+    for (const StripRun& r : sc.runs) {
+        if (r.dom != idx || (int)r.axis != axis) continue;
+        if (c < cap && runs) {
+            runs[4 * c] = r.first; runs[4 * c + 1] = r.count; runs[4 * c + 2] = r.d1; runs[4 * c + 3] = r.d2;
+        }
+        c++;
+    }
+    *n = c;
+    return PSTD_OK;
 }
 
 int pstd_scene_domain_count(pstd_kernel* h, int32_t* n) {
@@ -716,34 +947,46 @@ int pstd_scene_attenuation(pstd_kernel* h, int32_t idx, float* ax_p, float* ax_v
         pml_profile(sc.s, vel, asc, prof);
         for (int i = 0; i < n; i++) dst[i] = (float)prof[i];
     };
-    bool pml = d.pml;
-    fill(ax_p, d.nx, pml && d.att_x, false, d.asc_x);
-    fill(ax_v, d.nx + 1, pml && d.att_x, true, d.asc_x);
-    fill(ay_p, d.ny, pml && d.att_y, false, d.asc_y);
-    fill(ay_v, d.ny + 1, pml && d.att_y, true, d.asc_y);
+    fill(ax_p, d.nx, d.pml && d.att_x, false, d.asc_x);
+    fill(ax_v, d.nx + 1, d.pml && d.att_x, true, d.asc_x);
+    fill(ay_p, d.ny, d.pml && d.att_y, false, d.asc_y);
+    fill(ay_v, d.ny + 1, d.pml && d.att_y, true, d.asc_y);
     return PSTD_OK;
 }
 
-int pstd_profile_passes(pstd_kernel* h, int32_t n_steps, void* stream, float* ms_x, float* ms_y, int32_t* lx,
-                        int32_t* ly) {
-    NEED(h);
+int pstd_profile_passes(pstd_kernel* h, int32_t n_steps, void* stream, float* ms_stage, float* ms_total,
+                        int32_t* stage_launches, int32_t* total_launches) {
+    NEED_DEVICE(h);
     GUARD({
         auto* k = h->k.get();
         cudaStream_t st = stream ? (cudaStream_t)stream : k->stream;
-        std::vector<std::pair<cudaEvent_t, cudaEvent_t>> xe, ye;
+        std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev;
+        cudaEvent_t a, b;
+        CK(cudaEventCreate(&a));
+        CK(cudaEventCreate(&b));
+        CK(cudaEventRecord(a, st));
         for (int i = 0; i < n_steps; i++) {
-            k->enqueue_step(k->cur, st, &xe, &ye);
+            k->enqueue_step(k->cur, st, false, &ev);
             k->cur = (k->cur + 2) % 3;
             k->steps++;
         }
+        CK(cudaEventRecord(b, st));
         CK(cudaStreamSynchronize(st));
-        float tx = 0, ty = 0;
-        for (auto& p : xe) { float m; CK(cudaEventElapsedTime(&m, p.first, p.second)); tx += m; cudaEventDestroy(p.first); cudaEventDestroy(p.second); }
-        for (auto& p : ye) { float m; CK(cudaEventElapsedTime(&m, p.first, p.second)); ty += m; cudaEventDestroy(p.first); cudaEventDestroy(p.second); }
-        if (ms_x) *ms_x = tx;
-        if (ms_y) *ms_y = ty;
-        if (lx) *lx = (int32_t)(n_steps * 6 * k->xgroups.size());
-        if (ly) *ly = (int32_t)(n_steps * 6 * k->ygroups.size());
+        float ts = 0, tt = 0;
+        for (auto& p : ev) {
+            float m;
+            CK(cudaEventElapsedTime(&m, p.first, p.second));
+            ts += m;
+            cudaEventDestroy(p.first);
+            cudaEventDestroy(p.second);
+        }
+        CK(cudaEventElapsedTime(&tt, a, b));
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        if (ms_stage) *ms_stage = ts;
+        if (ms_total) *ms_total = tt;
+        if (stage_launches) *stage_launches = (int32_t)(n_steps * 6 * k->buckets.size());
+        if (total_launches) *total_launches = n_steps * k->launches_per_step();
         return PSTD_OK;
     })
 }
@@ -753,6 +996,18 @@ int pstd_work_counts(pstd_kernel* h, int64_t* cells, int64_t* air, int32_t* laun
     if (cells) *cells = h->k->cells;
     if (air) *air = h->k->air_cells;
     if (launches) *launches = h->k->launches_per_step();
+    return PSTD_OK;
+}
+
+int pstd_plan_info(pstd_kernel* h, char* buf, int32_t cap) {
+    NEED_DEVICE(h);
+    std::string s;
+    for (auto& b : h->k->buckets)
+        s += "L=" + std::to_string(b.L) + " jobs=" + std::to_string(b.n) + " variant=" + b.var->name + b.choice + "\n";
+    if (buf && cap > 0) {
+        std::strncpy(buf, s.c_str(), (size_t)cap - 1);
+        buf[cap - 1] = 0;
+    }
     return PSTD_OK;
 }
 

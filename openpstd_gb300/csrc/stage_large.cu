@@ -1,0 +1,18 @@
+// stage kernel variants for transform length 2048
+#include "stage_kernel.cuh"
+
+namespace pstd {
+
+const StageVariant* stage_variants_large(int L, int* n) {
+    static const StageVariant v2048[] = {
+        make_variant<Cfg<2048, 4, 256, 3, 16, 16, 8>>("L2048 cs4 nt256 r16.16.8"),
+        make_variant<Cfg<2048, 8, 512, 1, 16, 16, 8>>("L2048 cs8 nt512 r16.16.8"),
+        make_variant<Cfg<2048, 4, 256, 3, 8, 8, 8, 4>>("L2048 cs4 nt256 r8.8.8.4"),
+    };
+    switch (L) {
+        case 2048: *n = 3; return v2048;
+        default: *n = 0; return nullptr;
+    }
+}
+
+}  // namespace pstd

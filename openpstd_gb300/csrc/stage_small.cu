@@ -1,0 +1,30 @@
+// stage kernel variants for transform lengths 32 .. 256
+#include "stage_kernel.cuh"
+
+namespace pstd {
+
+const StageVariant* stage_variants_small(int L, int* n) {
+    static const StageVariant v32[] = {
+        make_variant<Cfg<32, 16, 64, 8, 8, 4>>("L32 cs16 nt64 r8.4"),
+    };
+    static const StageVariant v64[] = {
+        make_variant<Cfg<64, 16, 128, 6, 8, 8>>("L64 cs16 nt128 r8.8"),
+    };
+    static const StageVariant v128[] = {
+        make_variant<Cfg<128, 16, 128, 6, 16, 8>>("L128 cs16 nt128 r16.8"),
+        make_variant<Cfg<128, 8, 64, 8, 16, 8>>("L128 cs8 nt64 r16.8"),
+    };
+    static const StageVariant v256[] = {
+        make_variant<Cfg<256, 16, 256, 3, 16, 16>>("L256 cs16 nt256 r16.16"),
+        make_variant<Cfg<256, 8, 128, 5, 16, 16>>("L256 cs8 nt128 r16.16"),
+    };
+    switch (L) {
+        case 32: *n = 1; return v32;
+        case 64: *n = 1; return v64;
+        case 128: *n = 2; return v128;
+        case 256: *n = 2; return v256;
+        default: *n = 0; return nullptr;
+    }
+}
+
+}  // namespace pstd

@@ -238,12 +238,18 @@ class PSTDKernel(KernelInterface):
         return out
 
     def profile_passes(self, n_steps: int, stream: Optional[int] = None):
-        mx, my = ctypes.c_float(), ctypes.c_float()
-        lx, ly = ctypes.c_int32(), ctypes.c_int32()
+        """Advance n_steps with CUDA events around every RK stage."""
+        ms, mt = ctypes.c_float(), ctypes.c_float()
+        ls, lt = ctypes.c_int32(), ctypes.c_int32()
         _lib.check(_lib.lib().pstd_profile_passes(self._need(), int(n_steps), ctypes.c_void_p(stream) if stream else None,
-                                                  ctypes.byref(mx), ctypes.byref(my), ctypes.byref(lx),
-                                                  ctypes.byref(ly)))
-        return {"ms_x": mx.value, "ms_y": my.value, "launches_x": lx.value, "launches_y": ly.value}
+                                                  ctypes.byref(ms), ctypes.byref(mt), ctypes.byref(ls),
+                                                  ctypes.byref(lt)))
+        return {"ms_stage": ms.value, "ms_total": mt.value, "stage_launches": ls.value, "total_launches": lt.value}
+
+    def plan_info(self) -> str:
+        buf = ctypes.create_string_buffer(8192)
+        _lib.check(_lib.lib().pstd_plan_info(self._need(), buf, 8192))
+        return buf.value.decode()
 
     def work_counts(self):
         c, a = ctypes.c_int64(), ctypes.c_int64()
