@@ -16,7 +16,9 @@ struct StageArgs {
     const float* fixed;     // fields of rigid domains
     const float* p0;        // per-domain p0 read at the first stage (initial / stale)
     const int* first_step;  // 1 while the very first step runs
-    const float2* filt;     // derivative filters (position order)
+    const float2* filt;     // derivative filters (position order); jobs index them by dtab
+    const float2* filt_p;   // this bucket's pressure and velocity filters (persistent form)
+    const float2* filt_v;
     const float* win;       // window coefficients
     const float2* tw;       // twiddles exp(-2 pi i j / L), j < L
     const float* att;       // PML attenuation profiles
@@ -28,6 +30,7 @@ struct StageArgs {
 struct StageVariant {
     int L, CS, NT, smem, np;
     int r[4];                                                   // radix of each pass
+    bool persistent;                                            // warp-specialised persistent form
     cudaError_t (*launch)(int n_jobs, const StageArgs& a, cudaStream_t st);
     cudaError_t (*prepare)();
     const char* name;

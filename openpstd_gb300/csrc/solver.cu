@@ -103,6 +103,7 @@ struct Bucket {
     const StageVariant* var = nullptr;
     int off = 0, n = 0;            // jobs in djobs
     int tw_off = 0;                // float2 offset of the twiddles in dtw
+    int fp_off = 0, fv_off = 0;    // float2 offsets of the pressure / velocity filters
     std::string choice;            // autotune record
 };
 
@@ -448,7 +449,7 @@ struct Kernel {
                                 " speakers, " + std::to_string(sc.receivers.size()) + " receivers; stage kernels:" + choice);
     }
 
-    StageArgs stage_args(int c, int k, const DevJob* jobs, const float2* twp) {
+    StageArgs stage_args(int c, int k, const DevJob* jobs, const float2* twp, int fp = 0, int fv = 0) {
         const int A = (c + 1) % 3, B = (c + 2) % 3;
         StageArgs a;
         a.jobs = jobs;
@@ -460,6 +461,8 @@ struct Kernel {
         a.p0 = p0.p;
         a.first_step = first_step.p;
         a.filt = dfilt.p;
+        a.filt_p = dfilt.p + fp;
+        a.filt_v = dfilt.p + fv;
         a.win = dwin.p;
         a.tw = twp;
         a.att = datt.p;
@@ -482,10 +485,12 @@ struct Kernel {
                 int nv = stage_variants(b.L, &vs);
                 if (nv <= 1) continue;
                 std::vector<std::vector<DevJob>> all(nv);
-                std::vector<int> twv(nv);
+                std::vector<int> twv(nv), fpv(nv), fvv(nv);
                 for (int i = 0; i < nv; i++) {
                     all[i] = make_jobs(b.L, &vs[i], false);
                     twv[i] = twiddles_of(&vs[i]);
+                    fpv[i] = filter_of(b.L, false, &vs[i]);
+                    fvv[i] = filter_of(b.L, true, &vs[i]);
                 }
                 upload_tables();
                 float best = 1e30f;
@@ -498,7 +503,7 @@ struct Kernel {
                     if (all[i].empty()) continue;
                     DevBuf<DevJob> tj;
                     tj.upload(all[i]);
-                    StageArgs a = stage_args(cur, 1, tj.p, dtw.p + twv[i]);
+                    StageArgs a = stage_args(cur, 1, tj.p, dtw.p + twv[i], fpv[i], fvv[i]);
                     for (int w = 0; w < 2; w++) CK(vs[i].launch((int)all[i].size(), a, stream));
                     CK(cudaEventRecord(e0, stream));
                     const int reps = 5;
@@ -524,6 +529,8 @@ struct Kernel {
             auto& b = buckets[i];
             auto js = make_jobs(b.L, b.var, i + 1 == buckets.size());
             b.tw_off = twiddles_of(b.var);
+            b.fp_off = filter_of(b.L, false, b.var);
+            b.fv_off = filter_of(b.L, true, b.var);
             b.off = (int)jobs.size();
             b.n = (int)js.size();
             jobs.insert(jobs.end(), js.begin(), js.end());
@@ -575,7 +582,7 @@ struct Kernel {
                     auto& b = buckets[i];
                     cudaStream_t s = i == 0 ? st : side[i];
                     if (i > 0) CK(cudaStreamWaitEvent(s, fork, 0));
-                    StageArgs a = stage_args(c, k, djobs.p + b.off, dtw.p + b.tw_off);
+                    StageArgs a = stage_args(c, k, djobs.p + b.off, dtw.p + b.tw_off, b.fp_off, b.fv_off);
                     CK(b.var->launch(b.n, a, s));
                     if (i > 0) {
                         cudaEvent_t j = mk();
@@ -586,7 +593,7 @@ struct Kernel {
                 for (auto j : joins) CK(cudaStreamWaitEvent(st, j, 0));
             } else {
                 for (auto& b : buckets) {
-                    StageArgs a = stage_args(c, k, djobs.p + b.off, dtw.p + b.tw_off);
+                    StageArgs a = stage_args(c, k, djobs.p + b.off, dtw.p + b.tw_off, b.fp_off, b.fv_off);
                     CK(b.var->launch(b.n, a, st));
                 }
             }

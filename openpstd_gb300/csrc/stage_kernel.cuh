@@ -1,9 +1,10 @@
 // stage_kernel.cuh -- one RK stage of the strip-derivative solve, sm_103a.
 //
-// A CTA takes one job: up to 2*CS adjacent strips (rows for x, columns for
-// y) of one domain sharing both interface neighbours, and computes for each
-// the reference's windowed Fourier derivative (kernel/core/kernel_functions.cpp:
-// 123-318) fused with the RK stage update (kernel/Solver.cpp:162-182):
+// A job is up to 2*CS adjacent strips (rows for x, columns for y) of one
+// domain sharing both interface neighbours.  For each strip the kernels
+// compute the reference's windowed Fourier derivative (kernel/core/
+// kernel_functions.cpp:123-318) fused with the RK stage update
+// (kernel/Solver.cpp:162-182):
 //
 //   1. gather: strip + the two W-wide interface bands of the neighbours
 //      (reflected / transmitted and windowed, kernel/core/kernel_functions.cpp:
@@ -11,14 +12,23 @@
 //      in shared memory; p0 is formed as px + py of the previous stage while
 //      loading;
 //   2. forward complex FFT of length L in place (decimation in frequency,
-//      radix 16/8/4/2 butterflies in registers, twiddles from an FP64-built
-//      table), output in digit-reversed position order;
+//      radix 16/8/4/2 butterflies in registers, per-pass twiddle tables built
+//      in FP64), output in digit-reversed position order;
 //   3. multiply by the Hermitian-extended derivative filter i k e^{-/+ i k dx/2}
 //      (1/L folded in) stored in the same position order, fused with the last
 //      forward and the first inverse pass;
 //   4. inverse FFT (decimation in time), natural order;
 //   5. epilogue: slice W..W+n and RK-update against the stage-start set
 //      (vx/vy get the PML multiply of the sixth stage here).
+//
+// Two kernel forms share these steps:
+//   stage_kernel  -- one CTA per job, all threads do every step;
+//   stage_ws      -- persistent and warp specialised: per SM one CTA walks a
+//                    list of jobs; memory warps gather job j+1 and write back
+//                    job j-1 while FFT warps transform job j (two shared-
+//                    memory buffers handed over with named barriers); the
+//                    twiddle tables and both derivative filters are staged in
+//                    shared memory once per CTA.
 //
 // Packing two real strips into one complex strip is exact in real
 // arithmetic: the filter is Hermitian, so the operator is real and acts on
@@ -123,10 +133,12 @@ struct DFT<16, INV> {
     }
 };
 
-// ---------------------------------------------------------------- variant
-template <int L_, int CS_, int NT_, int MINB_, int R0_, int R1_, int R2_ = 0, int R3_ = 0>
+// ---------------------------------------------------------------- variants
+// Plain form: L, complex strips per CTA, threads, min CTAs per SM, radices.
+// Persistent form (NTP > 0): NT FFT threads + NTP memory threads.
+template <int L_, int CS_, int NT_, int MINB_, int R0_, int R1_, int R2_ = 0, int R3_ = 0, int NTP_ = 0>
 struct Cfg {
-    static constexpr int L = L_, CS = CS_, NT = NT_, MINB = MINB_;
+    static constexpr int L = L_, CS = CS_, NT = NT_, MINB = MINB_, NTP = NTP_;
     static constexpr int R0 = R0_, R1 = R1_, R2 = R2_, R3 = R3_;
     static constexpr int NP = R3_ ? 4 : (R2_ ? 3 : 2);
     static_assert(R0 * R1 * (R2 ? R2 : 1) * (R3 ? R3 : 1) == L, "radix plan must multiply to L");
@@ -134,32 +146,51 @@ struct Cfg {
     // half-warp touches at one offset fall in distinct bank pairs
     static constexpr int PAD = CS >= 16 ? 1 : 16 / CS;
     static constexpr int SP = L + PAD;
-    static constexpr int SMEM = CS * SP * 8;
+    static constexpr int BUF = CS * SP;            // float2 per job buffer
+    // twiddle table: one [n1][k] block of M entries per pass but the last
+    static constexpr int M1 = L / R0, M2 = M1 / R1;
+    static constexpr int TWN = NP == 2 ? L : (NP == 3 ? L + M1 : L + M1 + M2);
+    static constexpr int SMEM = NTP ? (2 * BUF + TWN + 2 * L) * 8 : BUF * 8;
 };
 
-// Twiddles of a pass with block size M and radix R live in a table
-// [n1][k] = exp(-2 pi i n1 k / M), n1 < M/R, k < R (k = 0 included so a row
-// is R float2 = R/2 aligned 16-byte loads); TOFF is the pass' offset.
-template <int R>
-__device__ __forceinline__ void load_twiddles(const float2* __restrict__ row, float2 (&w)[R]) {
+// group-local barrier: BAR 0 = the whole CTA, else a named barrier of NTH threads
+template <int BAR, int NTH>
+__device__ __forceinline__ void group_sync() {
+    if constexpr (BAR == 0) __syncthreads();
+    else asm volatile("bar.sync %0, %1;" ::"n"(BAR), "n"(NTH) : "memory");
+}
+__device__ __forceinline__ void bar_sync(int id, int n) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory"); }
+__device__ __forceinline__ void bar_arrive(int id, int n) { asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(n) : "memory"); }
+
+template <bool SMT, class T>
+__device__ __forceinline__ T tload(const T* p) {   // table load: shared (SMT) or read-only global
+    if constexpr (SMT) return *p;
+    else return __ldg(p);
+}
+
+// Twiddles of a pass with block size M and radix R: table [n1][k] =
+// exp(-2 pi i n1 k / M), n1 < M/R, k < R (k = 0 included, so a row is R
+// float2 read as R/2 16-byte loads).
+template <int R, bool SMT>
+__device__ __forceinline__ void load_twiddles(const float2* row, float2 (&w)[R]) {
     const float4* t4 = reinterpret_cast<const float4*>(row);
 #pragma unroll
     for (int h = 0; h < R / 2; h++) {
-        const float4 v = __ldg(t4 + h);
+        const float4 v = tload<SMT>(t4 + h);
         w[2 * h] = make_float2(v.x, v.y);
         w[2 * h + 1] = make_float2(v.z, v.w);
     }
 }
 
-template <class C, int R, int M, int TOFF>
-__device__ __forceinline__ void fwd_pass(float2* sm, const float2* __restrict__ tw) {
+template <class C, int R, int M, int TOFF, int NTH, bool SMT>
+__device__ __forceinline__ void fwd_pass(float2* sm, const float2* tw, int tid) {
     constexpr int Q = M / R;
     constexpr int ITEMS = C::CS * (C::L / R);
-    for (int it = threadIdx.x; it < ITEMS; it += C::NT) {
+    for (int it = tid; it < ITEMS; it += NTH) {
         const int cs = it % C::CS, b = it / C::CS;
         const int blk = b / Q, n1 = b % Q;
         float2 w[R];
-        if (Q > 1) load_twiddles<R>(tw + TOFF + n1 * R, w);
+        if (Q > 1) load_twiddles<R, SMT>(tw + TOFF + n1 * R, w);
         float2* base = sm + cs * C::SP + blk * M + n1;
         float2 x[R];
 #pragma unroll
@@ -174,15 +205,15 @@ __device__ __forceinline__ void fwd_pass(float2* sm, const float2* __restrict__ 
     }
 }
 
-template <class C, int R, int M, int TOFF>
-__device__ __forceinline__ void inv_pass(float2* sm, const float2* __restrict__ tw) {
+template <class C, int R, int M, int TOFF, int NTH, bool SMT>
+__device__ __forceinline__ void inv_pass(float2* sm, const float2* tw, int tid) {
     constexpr int Q = M / R;
     constexpr int ITEMS = C::CS * (C::L / R);
-    for (int it = threadIdx.x; it < ITEMS; it += C::NT) {
+    for (int it = tid; it < ITEMS; it += NTH) {
         const int cs = it % C::CS, b = it / C::CS;
         const int blk = b / Q, n1 = b % Q;
         float2 w[R];
-        if (Q > 1) load_twiddles<R>(tw + TOFF + n1 * R, w);
+        if (Q > 1) load_twiddles<R, SMT>(tw + TOFF + n1 * R, w);
         float2* base = sm + cs * C::SP + blk * M + n1;
         float2 x[R];
 #pragma unroll
@@ -197,59 +228,65 @@ __device__ __forceinline__ void inv_pass(float2* sm, const float2* __restrict__ 
     }
 }
 
-template <class C, int R>
-__device__ __forceinline__ void mid_pass(float2* sm, const float2* __restrict__ filt) {
+// last forward pass (blocks of R contiguous positions), filter, first inverse pass
+template <class C, int R, int NTH, bool SMT>
+__device__ __forceinline__ void mid_pass(float2* sm, const float2* filt, int tid) {
     constexpr int ITEMS = C::CS * (C::L / R);
-    for (int it = threadIdx.x; it < ITEMS; it += C::NT) {
+    for (int it = tid; it < ITEMS; it += NTH) {
         const int cs = it % C::CS, blk = it / C::CS;
         float2* base = sm + cs * C::SP + blk * R;
-        float2 x[R];
+        float2 f[R], x[R];
+#pragma unroll
+        for (int h = 0; h < R / 2; h++) {
+            const float4 v = tload<SMT>(reinterpret_cast<const float4*>(filt + blk * R) + h);
+            f[2 * h] = make_float2(v.x, v.y);
+            f[2 * h + 1] = make_float2(v.z, v.w);
+        }
 #pragma unroll
         for (int q = 0; q < R; q++) x[q] = base[q];
         DFT<R, false>::run(x);
 #pragma unroll
-        for (int k = 0; k < R; k++) x[k] = cmul(x[k], __ldg(&filt[blk * R + k]));
+        for (int k = 0; k < R; k++) x[k] = cmul(x[k], f[k]);
         DFT<R, true>::run(x);
 #pragma unroll
         for (int q = 0; q < R; q++) base[q] = x[q];
     }
 }
 
-template <class C>
-__device__ __forceinline__ void convolve(float2* sm, const float2* __restrict__ tw, const float2* __restrict__ filt) {
-    constexpr int M0 = C::L, M1 = M0 / C::R0;
-    constexpr int T0 = 0, T1 = M0;   // pass table offsets (a pass' table holds M entries)
+template <class C, int NTH, int BAR, bool SMT>
+__device__ __forceinline__ void convolve(float2* sm, const float2* tw, const float2* filt, int tid) {
+    constexpr int M0 = C::L, M1 = C::M1, M2 = C::M2;
+    constexpr int T0 = 0, T1 = M0, T2 = M0 + M1;
     if constexpr (C::NP == 2) {
-        fwd_pass<C, C::R0, M0, T0>(sm, tw);
-        __syncthreads();
-        mid_pass<C, C::R1>(sm, filt);
-        __syncthreads();
-        inv_pass<C, C::R0, M0, T0>(sm, tw);
+        fwd_pass<C, C::R0, M0, T0, NTH, SMT>(sm, tw, tid);
+        group_sync<BAR, NTH>();
+        mid_pass<C, C::R1, NTH, SMT>(sm, filt, tid);
+        group_sync<BAR, NTH>();
+        inv_pass<C, C::R0, M0, T0, NTH, SMT>(sm, tw, tid);
     } else if constexpr (C::NP == 3) {
-        fwd_pass<C, C::R0, M0, T0>(sm, tw);
-        __syncthreads();
-        fwd_pass<C, C::R1, M1, T1>(sm, tw);
-        __syncthreads();
-        mid_pass<C, C::R2>(sm, filt);
-        __syncthreads();
-        inv_pass<C, C::R1, M1, T1>(sm, tw);
-        __syncthreads();
-        inv_pass<C, C::R0, M0, T0>(sm, tw);
+        fwd_pass<C, C::R0, M0, T0, NTH, SMT>(sm, tw, tid);
+        group_sync<BAR, NTH>();
+        fwd_pass<C, C::R1, M1, T1, NTH, SMT>(sm, tw, tid);
+        group_sync<BAR, NTH>();
+        mid_pass<C, C::R2, NTH, SMT>(sm, filt, tid);
+        group_sync<BAR, NTH>();
+        inv_pass<C, C::R1, M1, T1, NTH, SMT>(sm, tw, tid);
+        group_sync<BAR, NTH>();
+        inv_pass<C, C::R0, M0, T0, NTH, SMT>(sm, tw, tid);
     } else {
-        constexpr int M2 = M1 / C::R1, T2 = M0 + M1;
-        fwd_pass<C, C::R0, M0, T0>(sm, tw);
-        __syncthreads();
-        fwd_pass<C, C::R1, M1, T1>(sm, tw);
-        __syncthreads();
-        fwd_pass<C, C::R2, M2, T2>(sm, tw);
-        __syncthreads();
-        mid_pass<C, C::R3>(sm, filt);
-        __syncthreads();
-        inv_pass<C, C::R2, M2, T2>(sm, tw);
-        __syncthreads();
-        inv_pass<C, C::R1, M1, T1>(sm, tw);
-        __syncthreads();
-        inv_pass<C, C::R0, M0, T0>(sm, tw);
+        fwd_pass<C, C::R0, M0, T0, NTH, SMT>(sm, tw, tid);
+        group_sync<BAR, NTH>();
+        fwd_pass<C, C::R1, M1, T1, NTH, SMT>(sm, tw, tid);
+        group_sync<BAR, NTH>();
+        fwd_pass<C, C::R2, M2, T2, NTH, SMT>(sm, tw, tid);
+        group_sync<BAR, NTH>();
+        mid_pass<C, C::R3, NTH, SMT>(sm, filt, tid);
+        group_sync<BAR, NTH>();
+        inv_pass<C, C::R2, M2, T2, NTH, SMT>(sm, tw, tid);
+        group_sync<BAR, NTH>();
+        inv_pass<C, C::R1, M1, T1, NTH, SMT>(sm, tw, tid);
+        group_sync<BAR, NTH>();
+        inv_pass<C, C::R0, M0, T0, NTH, SMT>(sm, tw, tid);
     }
 }
 
@@ -305,30 +342,30 @@ __device__ __forceinline__ float4 add4(float4 a, float4 b) {
 
 // Carry the fields of a non-updated axis through the stage: the derivative
 // array keeps its zero content, so the RK update returns the stage-start value.
-static __device__ void copy_axis(const StageArgs& A, const DevDomain& D, bool ydir) {
-    const int nt = blockDim.x;
+template <int NTH>
+__device__ void copy_axis(const StageArgs& A, const DevDomain& D, bool ydir, int tid) {
     if (!ydir) {
-        for (int k = threadIdx.x; k < D.ny * (D.nx + 1); k += nt) {
+        for (int k = tid; k < D.ny * (D.nx + 1); k += NTH) {
             const int r = k / (D.nx + 1), i = k - r * (D.nx + 1);
             const long long e = D.o_vx + (long long)r * D.pitch_vx + i;
             float v = A.prev[e];
             if (A.last && D.att_xv >= 0) v = __fmul_rn(v, A.att[D.att_xv + i]);
             A.out[e] = v;
         }
-        for (int k = threadIdx.x; k < D.ny * D.nx; k += nt) {
+        for (int k = tid; k < D.ny * D.nx; k += NTH) {
             const int r = k / D.nx, i = k - r * D.nx;
             const long long e = D.o_px + (long long)r * D.pitch_p + i;
             A.out[e] = A.prev[e];
         }
     } else {
-        for (int k = threadIdx.x; k < (D.ny + 1) * D.nx; k += nt) {
+        for (int k = tid; k < (D.ny + 1) * D.nx; k += NTH) {
             const int r = k / D.nx, i = k - r * D.nx;
             const long long e = D.o_vy + (long long)r * D.pitch_vy + i;
             float v = A.prev[e];
             if (A.last && D.att_yv >= 0) v = __fmul_rn(v, A.att[D.att_yv + r]);
             A.out[e] = v;
         }
-        for (int k = threadIdx.x; k < D.ny * D.nx; k += nt) {
+        for (int k = tid; k < D.ny * D.nx; k += NTH) {
             const int r = k / D.nx, i = k - r * D.nx;
             const long long e = D.o_py + (long long)r * D.pitch_p + i;
             A.out[e] = A.prev[e];
@@ -336,43 +373,34 @@ static __device__ void copy_axis(const StageArgs& A, const DevDomain& D, bool yd
     }
 }
 
-template <class C>
-__global__ void __launch_bounds__(C::NT, C::MINB) stage_kernel(StageArgs A) {
-    constexpr int CS = C::CS, NT = C::NT, SP = C::SP, L = C::L;
-    constexpr int S2 = 2 * CS;
-    extern __shared__ float2 sm[];
-    float* smf = reinterpret_cast<float*>(sm);
-    const DevJob job = A.jobs[blockIdx.x];
-    const DevDomain dom = A.doms[job.dom];
-    const bool ydir = job.kind & JK_Y;
-    if (job.kind & JK_COPY) {
-        copy_axis(A, dom, ydir);
-        return;
-    }
-    const bool vel = job.kind & JK_VEL;
-    const bool first = *A.first_step != 0;
-    const int W = job.W;
-    const int n = (ydir ? dom.ny : dom.nx) + (vel ? 1 : 0);   // strip length
-    const int count = job.count;
-    const Src S = strip_source(A, dom, vel, ydir, first);
-
-    // ---- 1. gather -------------------------------------------------------
-    constexpr int NW = NT / 32;                   // warps
+// ---- step 1: strips + bands + padding of one job into `sm` (NTH threads)
+template <class C, int NTH>
+__device__ __forceinline__ void gather(float2* sm, const StageArgs& A, const DevJob& job, const DevDomain& dom,
+                                       bool first, int tid) {
+    constexpr int CS = C::CS, SP = C::SP, L = C::L, S2 = 2 * CS;
+    constexpr int NW = NTH / 32;
     constexpr int WPP = NW >= CS ? NW / CS : 1;   // warps per strip pair
     constexpr int PST = NW / WPP;                 // strip pairs in flight
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float* smf = reinterpret_cast<float*>(sm);
+    const int warp = tid >> 5, lane = tid & 31;
+    const bool vel = job.kind & JK_VEL;
+    const bool ydir = job.kind & JK_Y;
+    const int W = job.W;
+    const int n = (ydir ? dom.ny : dom.nx) + (vel ? 1 : 0);
+    const int count = job.count;
+    const Src S = strip_source(A, dom, vel, ydir, first);
     if (!ydir) {
-        // row pairs (2cs, 2cs+1), 16-byte loads, two chunks per lane in flight
+        // row pairs (2cs, 2cs+1), 16-byte loads, four chunks per lane in flight
         const int chunks = (n + 3) >> 2;
         for (int cs = warp / WPP; cs < CS; cs += PST) {
             const int s0 = 2 * cs;
             const float* a0 = S.a + (long long)(job.first + s0) * S.pitch;
             const float* b0 = S.b ? S.b + (long long)(job.first + s0) * S.pitch : nullptr;
             const bool h0 = s0 < count, h1 = s0 + 1 < count;
-            for (int c0 = (warp % WPP) * 32 + lane; c0 < chunks; c0 += 2 * WPP * 32) {
-                float4 u[2], v[2];
+            for (int c0 = (warp % WPP) * 32 + lane; c0 < chunks; c0 += 4 * WPP * 32) {
+                float4 u[4], v[4];
 #pragma unroll
-                for (int q = 0; q < 2; q++) {
+                for (int q = 0; q < 4; q++) {
                     const int c = c0 + q * WPP * 32, i = c << 2;
                     u[q] = v[q] = make_float4(0.f, 0.f, 0.f, 0.f);
                     if (c < chunks) {
@@ -381,7 +409,7 @@ __global__ void __launch_bounds__(C::NT, C::MINB) stage_kernel(StageArgs A) {
                     }
                 }
 #pragma unroll
-                for (int q = 0; q < 2; q++) {
+                for (int q = 0; q < 4; q++) {
                     const int c = c0 + q * WPP * 32, i = c << 2;
                     if (c < chunks) {
                         float2* d = sm + cs * SP + W + i;
@@ -397,11 +425,11 @@ __global__ void __launch_bounds__(C::NT, C::MINB) stage_kernel(StageArgs A) {
         // columns: consecutive threads read consecutive columns of one row,
         // four elements per thread in flight
         const int total = S2 * n;
-        for (int f0 = threadIdx.x; f0 < total; f0 += 4 * NT) {
+        for (int f0 = tid; f0 < total; f0 += 4 * NTH) {
             float val[4];
 #pragma unroll
             for (int q = 0; q < 4; q++) {
-                const int f = f0 + q * NT;
+                const int f = f0 + q * NTH;
                 val[q] = 0.f;
                 if (f < total) {
                     const int s = f % S2, i = f / S2;
@@ -410,7 +438,7 @@ __global__ void __launch_bounds__(C::NT, C::MINB) stage_kernel(StageArgs A) {
             }
 #pragma unroll
             for (int q = 0; q < 4; q++) {
-                const int f = f0 + q * NT;
+                const int f = f0 + q * NTH;
                 if (f < total) {
                     const int s = f % S2, i = f / S2;
                     smf[2 * ((s >> 1) * SP + W + i) + (s & 1)] = val[q];
@@ -418,80 +446,87 @@ __global__ void __launch_bounds__(C::NT, C::MINB) stage_kernel(StageArgs A) {
             }
         }
     }
-    // interface bands and zero padding
-    {
-        const float* wl = A.win + job.wtab;          // window.head(W)
-        const float* wr = A.win + job.wtab + W + 1;  // window.tail(W)
-        Src S1{nullptr, nullptr, 0}, S3{nullptr, nullptr, 0};
-        int n1 = 0;
-        if (job.d1 >= 0) {
-            const DevDomain D1 = A.doms[job.d1];
-            S1 = strip_source(A, D1, vel, ydir, first);
-            n1 = (ydir ? D1.ny : D1.nx) + (vel ? 1 : 0);
-        }
-        if (job.d2 >= 0) S3 = strip_source(A, A.doms[job.d2], vel, ydir, first);
-        // bands: one warp per strip, lanes along the band
-        for (int s = warp; s < S2; s += NW) {
-            const bool live = s < count;
-            for (int j = lane; j < 2 * W; j += 32) {
-                float val = 0.f;
-                int pos;
-                if (j < W) {
-                    pos = j;
-                    if (live && job.d1 >= 0) {
-                        const int e1 = vel ? n1 - W - 1 + j : n1 - W + j;   // far end of the low neighbour
-                        const int m = vel ? W - j : W - 1 - j;              // mirrored own element
-                        float raw, mir;
-                        if (!ydir) {
-                            raw = S1.at((long long)(job.o1 + s) * S1.pitch + e1);
-                            mir = S.at((long long)(job.first + s) * S.pitch + m);
-                        } else {
-                            raw = S1.at((long long)e1 * S1.pitch + job.o1 + s);
-                            mir = S.at((long long)m * S.pitch + job.first + s);
-                        }
-                        val = band_value(raw, mir, job.T1, job.R1, wl[j]);
-                    }
-                } else {
-                    const int jj = j - W;
-                    pos = W + n + jj;
-                    if (live && job.d2 >= 0) {
-                        const int e2 = vel ? 1 + jj : jj;                   // near end of the high neighbour
-                        const int m = vel ? n - 2 - jj : n - 1 - jj;
-                        float raw, mir;
-                        if (!ydir) {
-                            raw = S3.at((long long)(job.o2 + s) * S3.pitch + e2);
-                            mir = S.at((long long)(job.first + s) * S.pitch + m);
-                        } else {
-                            raw = S3.at((long long)e2 * S3.pitch + job.o2 + s);
-                            mir = S.at((long long)m * S.pitch + job.first + s);
-                        }
-                        val = band_value(raw, mir, job.T2, job.R2, wr[jj]);
-                    }
-                }
-                smf[2 * ((s >> 1) * SP + pos) + (s & 1)] = val;
-            }
-        }
-        // zero padding [2W+n, L) of every complex strip
-        const int z0 = 2 * W + n;
-        for (int cs = warp; cs < CS; cs += NW)
-            for (int p = z0 + lane; p < L; p += 32) sm[cs * SP + p] = make_float2(0.f, 0.f);
+    // interface bands: one warp per strip, lanes along the band
+    const float* wl = A.win + job.wtab;          // window.head(W)
+    const float* wr = A.win + job.wtab + W + 1;  // window.tail(W)
+    Src S1{nullptr, nullptr, 0}, S3{nullptr, nullptr, 0};
+    int n1 = 0;
+    if (job.d1 >= 0) {
+        const DevDomain D1 = A.doms[job.d1];
+        S1 = strip_source(A, D1, vel, ydir, first);
+        n1 = (ydir ? D1.ny : D1.nx) + (vel ? 1 : 0);
     }
-    __syncthreads();
+    if (job.d2 >= 0) S3 = strip_source(A, A.doms[job.d2], vel, ydir, first);
+    for (int s = warp; s < S2; s += NW) {
+        const bool live = s < count;
+        for (int j = lane; j < 2 * W; j += 32) {
+            float val = 0.f;
+            int pos;
+            if (j < W) {
+                pos = j;
+                if (live && job.d1 >= 0) {
+                    const int e1 = vel ? n1 - W - 1 + j : n1 - W + j;   // far end of the low neighbour
+                    const int m = vel ? W - j : W - 1 - j;              // mirrored own element
+                    float raw, mir;
+                    if (!ydir) {
+                        raw = S1.at((long long)(job.o1 + s) * S1.pitch + e1);
+                        mir = S.at((long long)(job.first + s) * S.pitch + m);
+                    } else {
+                        raw = S1.at((long long)e1 * S1.pitch + job.o1 + s);
+                        mir = S.at((long long)m * S.pitch + job.first + s);
+                    }
+                    val = band_value(raw, mir, job.T1, job.R1, wl[j]);
+                }
+            } else {
+                const int jj = j - W;
+                pos = W + n + jj;
+                if (live && job.d2 >= 0) {
+                    const int e2 = vel ? 1 + jj : jj;                   // near end of the high neighbour
+                    const int m = vel ? n - 2 - jj : n - 1 - jj;
+                    float raw, mir;
+                    if (!ydir) {
+                        raw = S3.at((long long)(job.o2 + s) * S3.pitch + e2);
+                        mir = S.at((long long)(job.first + s) * S.pitch + m);
+                    } else {
+                        raw = S3.at((long long)e2 * S3.pitch + job.o2 + s);
+                        mir = S.at((long long)m * S.pitch + job.first + s);
+                    }
+                    val = band_value(raw, mir, job.T2, job.R2, wr[jj]);
+                }
+            }
+            smf[2 * ((s >> 1) * SP + pos) + (s & 1)] = val;
+        }
+    }
+    // zero padding [2W+n, L) of every complex strip
+    const int z0 = 2 * W + n;
+    for (int cs = warp; cs < CS; cs += NW)
+        for (int p = z0 + lane; p < L; p += 32) sm[cs * SP + p] = make_float2(0.f, 0.f);
+}
 
-    // ---- 2-4. FFT, derivative filter, inverse FFT -------------------------
-    convolve<C>(sm, A.tw, A.filt + job.dtab);
-    __syncthreads();
-
-    // ---- 5. epilogue -------------------------------------------------------
+// ---- step 5: slice, RK update, (sixth stage) PML on vx / vy
+template <class C, int NTH>
+__device__ __forceinline__ void epilogue(const float2* sm, const StageArgs& A, const DevJob& job, const DevDomain& dom,
+                                         int tid) {
+    constexpr int CS = C::CS, SP = C::SP, S2 = 2 * CS;
+    constexpr int NW = NTH / 32;
+    constexpr int WPP = NW >= CS ? NW / CS : 1;
+    constexpr int PST = NW / WPP;
+    const float* smf = reinterpret_cast<const float*>(sm);
+    const int warp = tid >> 5, lane = tid & 31;
+    const bool vel = job.kind & JK_VEL;
+    const bool ydir = job.kind & JK_Y;
+    const int W = job.W;
+    const int n = (ydir ? dom.ny : dom.nx) + (vel ? 1 : 0);
+    const int count = job.count;
     const float cdt = A.doms[job.dom].cdt[A.stage];
     const float rho = dom.rho;
+    const float c2 = dom.c2;
     const int nout = vel ? n - 1 : n + 1;   // cells (vel) or faces (pressure)
     long long fo;
     int fp, ao;
     if (!vel) { fo = ydir ? dom.o_vy : dom.o_vx; fp = ydir ? dom.pitch_vy : dom.pitch_vx; ao = ydir ? dom.att_yv : dom.att_xv; }
     else { fo = ydir ? dom.o_py : dom.o_px; fp = dom.pitch_p; ao = -1; }
     const bool att = A.last && ao >= 0;
-    const float c2 = dom.c2;
     if (!ydir) {
         for (int cs = warp / WPP; cs < CS; cs += PST) {
             const float2* srow = sm + cs * SP + W;
@@ -515,7 +550,7 @@ __global__ void __launch_bounds__(C::NT, C::MINB) stage_kernel(StageArgs A) {
             }
         }
     } else {
-        for (int f = threadIdx.x; f < S2 * nout; f += NT) {
+        for (int f = tid; f < S2 * nout; f += NTH) {
             const int s = f % S2, i = f / S2;
             if (s >= count) continue;
             const float dv = smf[2 * ((s >> 1) * SP + W + i) + (s & 1)];
@@ -532,22 +567,117 @@ __global__ void __launch_bounds__(C::NT, C::MINB) stage_kernel(StageArgs A) {
     }
 }
 
+// ---------------------------------------------------------------- plain form
+template <class C>
+__global__ void __launch_bounds__(C::NT, C::MINB) stage_kernel(StageArgs A) {
+    extern __shared__ float2 sm[];
+    const DevJob job = A.jobs[blockIdx.x];
+    const DevDomain dom = A.doms[job.dom];
+    if (job.kind & JK_COPY) {
+        copy_axis<C::NT>(A, dom, job.kind & JK_Y, threadIdx.x);
+        return;
+    }
+    const bool first = *A.first_step != 0;
+    gather<C, C::NT>(sm, A, job, dom, first, threadIdx.x);
+    __syncthreads();
+    convolve<C, C::NT, 0, false>(sm, A.tw, A.filt + job.dtab, threadIdx.x);
+    __syncthreads();
+    epilogue<C, C::NT>(sm, A, job, dom, threadIdx.x);
+}
+
+// ---------------------------------------------------------------- persistent form
+// named barriers: 1,2 buffer full; 3,4 buffer transformed; 5 FFT warps; 6 memory warps
+template <class C>
+__global__ void __launch_bounds__(C::NT + C::NTP, 1) stage_ws(StageArgs A, int n_jobs) {
+    constexpr int NTC = C::NT, NTP = C::NTP, ALL = C::NT + C::NTP;
+    extern __shared__ float2 sm[];
+    float2* tws = sm + 2 * C::BUF;
+    float2* flt = tws + C::TWN;
+    const int tid = threadIdx.x;
+    // stage the twiddle tables and both derivative filters once
+    {
+        const float4* s4 = reinterpret_cast<const float4*>(A.tw);
+        float4* d4 = reinterpret_cast<float4*>(tws);
+        for (int i = tid; i < C::TWN / 2; i += ALL) d4[i] = __ldg(s4 + i);
+        const float4* p4 = reinterpret_cast<const float4*>(A.filt_p);
+        const float4* v4 = reinterpret_cast<const float4*>(A.filt_v);
+        float4* f4 = reinterpret_cast<float4*>(flt);
+        for (int i = tid; i < C::L / 2; i += ALL) {
+            f4[i] = __ldg(p4 + i);
+            f4[C::L / 2 + i] = __ldg(v4 + i);
+        }
+    }
+    __syncthreads();
+    const int stride = gridDim.x;
+    const int mine = (int)blockIdx.x < n_jobs ? (n_jobs - 1 - (int)blockIdx.x) / stride + 1 : 0;
+    if (tid < NTC) {
+        // FFT warps
+        for (int k = 0; k < mine; k++) {
+            const int b = k & 1;
+            const int kind = A.jobs[blockIdx.x + k * stride].kind;
+            bar_sync(1 + b, ALL);
+            if (!(kind & JK_COPY))
+                convolve<C, NTC, 5, true>(sm + b * C::BUF, tws, flt + ((kind & JK_VEL) ? C::L : 0), tid);
+            bar_arrive(3 + b, ALL);
+        }
+    } else {
+        // memory warps: gather job k while the FFT warps transform job k-1,
+        // then write back job k-1
+        const int ptid = tid - NTC;
+        const bool first = *A.first_step != 0;
+        for (int k = 0; k <= mine; k++) {
+            if (k < mine) {
+                const int b = k & 1;
+                const DevJob job = A.jobs[blockIdx.x + k * stride];
+                if (!(job.kind & JK_COPY)) gather<C, NTP>(sm + b * C::BUF, A, job, A.doms[job.dom], first, ptid);
+                bar_arrive(1 + b, ALL);
+            }
+            if (k >= 1) {
+                const int b = (k - 1) & 1;
+                const DevJob job = A.jobs[blockIdx.x + (k - 1) * stride];
+                bar_sync(3 + b, ALL);
+                const DevDomain dom = A.doms[job.dom];
+                if (job.kind & JK_COPY) copy_axis<NTP>(A, dom, job.kind & JK_Y, ptid);
+                else epilogue<C, NTP>(sm + b * C::BUF, A, job, dom, ptid);
+                group_sync<6, NTP>();   // buffer b is gathered again at iteration k+1
+            }
+        }
+    }
+}
+
 template <class C>
 cudaError_t launch_stage_t(int n_jobs, const StageArgs& a, cudaStream_t st) {
-    stage_kernel<C><<<n_jobs, C::NT, C::SMEM, st>>>(a);
+    if constexpr (C::NTP > 0) {
+        static int grid = 0;
+        if (grid == 0) {
+            int dev, sms, per;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, stage_ws<C>, C::NT + C::NTP, C::SMEM);
+            grid = sms * (per > 0 ? per : 1);
+        }
+        const int g = n_jobs < grid ? n_jobs : grid;
+        stage_ws<C><<<g, C::NT + C::NTP, C::SMEM, st>>>(a, n_jobs);
+    } else {
+        stage_kernel<C><<<n_jobs, C::NT, C::SMEM, st>>>(a);
+    }
     return cudaGetLastError();
 }
 
 template <class C>
 cudaError_t prepare_stage_t() {
-    return cudaFuncSetAttribute(stage_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM);
+    if constexpr (C::NTP > 0)
+        return cudaFuncSetAttribute(stage_ws<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM);
+    else
+        return cudaFuncSetAttribute(stage_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM);
 }
 
 template <class C>
 StageVariant make_variant(const char* name) {
     StageVariant v;
-    v.L = C::L; v.CS = C::CS; v.NT = C::NT; v.smem = C::SMEM; v.np = C::NP;
+    v.L = C::L; v.CS = C::CS; v.NT = C::NT + C::NTP; v.smem = C::SMEM; v.np = C::NP;
     v.r[0] = C::R0; v.r[1] = C::R1; v.r[2] = C::R2; v.r[3] = C::R3;
+    v.persistent = C::NTP > 0;
     v.launch = &launch_stage_t<C>;
     v.prepare = &prepare_stage_t<C>;
     v.name = name;
