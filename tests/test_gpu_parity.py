@@ -3,7 +3,7 @@ restated, double = FP64 build), through the C ABI.
 
 Tolerances:
 * receiver time series: relative L2 <= 1e-5 against the float oracle and
-  against the FP64 oracle (the spec bar) wherever the float oracle is
+  against the FP64 oracle wherever the float oracle is
   itself within 1e-5/3 of FP64; receivers the wave has not reached carry
   only round-off, and there the GPU must stay within 3x the float oracle's
   distance to FP64;
