@@ -164,6 +164,17 @@ int pstd_get_receivers(pstd_kernel* k, int32_t first_step, int32_t n_steps, floa
  * to dst, row-major, dense.  n must equal the field's element count. */
 int pstd_snapshot(pstd_kernel* k, int32_t domain_index, int32_t field, float* dst, int64_t n);
 
+/* ---- batched solves (no reference counterpart) --------------------------
+ * Several independent scenes advanced together: every RK stage launches
+ * the stage kernel once per strip length over the strips of all scenes.
+ * Domains and receivers of the batch are numbered globally, scene after
+ * scene; pstd_advance / pstd_get_receivers / pstd_snapshot / scene
+ * inspection take these global indices.  pstd_run is single-scene only. */
+int pstd_create_batch(const pstd_config* configs, int32_t n_configs, const pstd_callbacks* log_cb, pstd_kernel** out);
+/* info[5] = {first global domain, domains, first global receiver, receivers, Framecount} */
+int pstd_batch_scene(pstd_kernel* k, int32_t scene, int32_t* info);
+int pstd_batch_size(pstd_kernel* k, int32_t* n_scenes, int32_t* n_receivers);
+
 /* ---- scene inspection (no reference counterpart; used for parity tests) - */
 typedef struct pstd_domain_info {
     int32_t id;

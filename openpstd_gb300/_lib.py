@@ -52,6 +52,9 @@ SIGNATURES = {
     "pstd_steps_done": (ctypes.c_int, [_vp, _P(_i32)]),
     "pstd_get_receivers": (ctypes.c_int, [_vp, _i32, _i32, _P(_f32)]),
     "pstd_snapshot": (ctypes.c_int, [_vp, _i32, _i32, _P(_f32), _i64]),
+    "pstd_create_batch": (ctypes.c_int, [_P(c_config), _i32, _P(c_callbacks), _P(_vp)]),
+    "pstd_batch_scene": (ctypes.c_int, [_vp, _i32, _P(_i32)]),
+    "pstd_batch_size": (ctypes.c_int, [_vp, _P(_i32), _P(_i32)]),
     "pstd_scene_build": (ctypes.c_int, [_P(c_config), _P(_vp)]),
     "pstd_scene_strip_runs": (ctypes.c_int, [_vp, _i32, _i32, _P(_i32), _i32, _P(_i32)]),
     "pstd_scene_domain_count": (ctypes.c_int, [_vp, _P(_i32)]),

@@ -31,6 +31,7 @@ struct DevDomain {
     int att_xp, att_xv, att_yp, att_yv;   // offsets into the attenuation table, -1 = none
     int pml;                              // PML domain (stale p0 at the first stage of a step)
     int fixed;                            // rigid: fields in the fixed buffer
+    int scene;                            // scene of a batch (index of its first-step flag)
     long long o_px, o_py, o_vx, o_vy;     // float offsets inside a state set (or the fixed buffer)
     long long o_p0;                       // float offset in the p0 array
     float rho;                            // domain density (float, as the reference)

@@ -15,7 +15,7 @@ struct StageArgs {
     float* out;             // new state
     const float* fixed;     // fields of rigid domains
     const float* p0;        // per-domain p0 read at the first stage (initial / stale)
-    const int* first_step;  // 1 while the very first step runs
+    const int* first_step;  // per scene: 1 while the scene's very first step runs
     const float2* filt;     // derivative filters (position order); jobs index them by dtab
     const float2* filt_p;   // this bucket's pressure and velocity filters (persistent form)
     const float2* filt_v;
@@ -40,7 +40,7 @@ struct StageVariant {
 int stage_variants(int L, const StageVariant** out);
 
 cudaError_t launch_pml_post(const int* doms_idx, int n, const DevDomain* doms, float* set, float* fixed, float* p0,
-                            const float* att, int* first_step, cudaStream_t st);
+                            const float* att, cudaStream_t st);
 cudaError_t launch_speakers(const DevDomain* doms, const int* x0, const int* y0, int n_dom, const DevSpeaker* spk,
                             int n_spk, float dx, float bw, float* set, float* fixed, float* p0, cudaStream_t st);
 cudaError_t launch_receivers(const DevReceiver* rec, int n_rec, const DevDomain* doms, const float* set, float* ring,

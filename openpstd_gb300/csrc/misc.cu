@@ -26,10 +26,9 @@ int stage_variants(int L, const StageVariant** out) {
 // kernel/core/Domain.cpp:716-725): keep p0 = px + py from before the multiply
 // (the reference does not recompute p0 after it), then px *= ax, py *= ay.
 // vx and vy of non-rigid domains were attenuated in the stage epilogue; rigid
-// domains (fields in the fixed buffer) get all four multiplies here.  Clears
-// the first-step flag.
+// domains (fields in the fixed buffer) get all four multiplies here.
 __global__ void pml_post_kernel(const int* idx, const DevDomain* doms, float* set, float* fixed, float* p0,
-                                const float* __restrict__ att, int* first_step) {
+                                const float* __restrict__ att) {
     const DevDomain d = doms[idx[blockIdx.y]];
     float* base = d.fixed ? fixed : set;
     const int stride = gridDim.x * blockDim.x;
@@ -54,7 +53,6 @@ __global__ void pml_post_kernel(const int* idx, const DevDomain* doms, float* se
             if (d.att_yv >= 0) base[e] = __fmul_rn(base[e], att[d.att_yv + r]);
         }
     }
-    if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) *first_step = 0;
 }
 
 // Gaussian speaker initial condition (kernel/core/Speaker.cpp:21-39) on every
@@ -118,9 +116,9 @@ __global__ void frame_kernel(const int* idx, const long long* dst_off, const Dev
 }
 
 cudaError_t launch_pml_post(const int* idx, int n, const DevDomain* doms, float* set, float* fixed, float* p0,
-                            const float* att, int* first_step, cudaStream_t st) {
+                            const float* att, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    pml_post_kernel<<<dim3(8, n), 256, 0, st>>>(idx, doms, set, fixed, p0, att, first_step);
+    pml_post_kernel<<<dim3(8, n), 256, 0, st>>>(idx, doms, set, fixed, p0, att);
     return cudaGetLastError();
 }
 

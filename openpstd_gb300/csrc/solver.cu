@@ -108,7 +108,10 @@ struct Bucket {
 };
 
 struct Kernel {
-    Scene sc;
+    std::vector<Scene> scenes;          // one per batch member (a single scene: one)
+    std::vector<int> dom_base;          // global index of each scene's first domain
+    std::vector<int> rec_base;          // global index of each scene's first receiver
+    std::vector<std::pair<int, int>> gdom;   // global domain -> (scene, local index)
     int device = 0;
     cudaStream_t stream = nullptr;
     std::vector<cudaStream_t> side;     // one per bucket, for concurrent capture
@@ -142,9 +145,9 @@ struct Kernel {
 
     // host-side tables
     std::vector<float> win;
-    std::map<int, int> win_off;
+    std::map<std::pair<int, int>, int> win_off;   // (W, patch error)
     std::vector<float2> filt;
-    std::map<std::tuple<int, int, int, int, int, int>, int> filt_off;   // (L, vel, radices)
+    std::map<std::tuple<int, int, int, int, int, int, float>, int> filt_off;   // (L, vel, radices, dx)
     std::vector<float2> tw;
     std::map<std::tuple<int, int, int, int, int>, int> tw_off;   // (L, radices)
 
@@ -170,29 +173,33 @@ struct Kernel {
     }
 
     // ---------------------------------------------------------------- tables
-    int window_of(int W) {
-        auto it = win_off.find(W);
+    const Domain& dom(int g) const { return scenes[gdom[g].first].doms[gdom[g].second]; }
+    const Scene& scene_of(int g) const { return scenes[gdom[g].first]; }
+
+    int window_of(int W, int patch) {
+        auto key = std::make_pair(W, patch);
+        auto it = win_off.find(key);
         if (it != win_off.end()) return it->second;
         int o = (int)win.size();
         // kernel/core/kernel_functions.cpp:327-333 (patch error cast to int)
-        double walpha = ((int)sc.s.patcherror - 40) / 20.0 + 1;
+        double walpha = (patch - 40) / 20.0 + 1;
         for (int i = -W; i <= W; i++) {
             double x = (double)i / W;
             double x6 = x * x * x * x * x * x;
             win.push_back((float)std::exp(-std::log(10.0) * walpha * x6));
         }
-        win_off[W] = o;
+        win_off[key] = o;
         return o;
     }
 
-    int filter_of(int L, bool vel, const StageVariant* v) {
-        auto key = std::make_tuple(L, (int)vel, v->r[0], v->r[1], v->r[2], v->r[3]);
+    int filter_of(int L, bool vel, const StageVariant* v, float dxf) {
+        auto key = std::make_tuple(L, (int)vel, v->r[0], v->r[1], v->r[2], v->r[3], dxf);
         auto it = filt_off.find(key);
         if (it != filt_off.end()) return it->second;
         int o = (int)filt.size();
         // kernel/core/WisdomCache.cpp:53-75: k_j = j (pi/dx)/(L/2) for bins
         // 0..L/2, factor exp(-/+ i k dx/2) * i k; Hermitian extension; 1/L
-        const double dx = (double)sc.s.dx;
+        const double dx = (double)dxf;
         const double kmax = M_PI / dx;
         std::vector<std::complex<double>> full(L);
         for (int j = 0; j <= L / 2; j++) {
@@ -236,62 +243,67 @@ struct Kernel {
         return o;
     }
 
-    int run_length(const StripRun& r) const {
+    static int run_length(const Scene& sc, const StripRun& r) {
         int n = sc.doms[r.dom].len(r.axis);
         return Scene::next_pow2(n + 2 * sc.window_for(n));
     }
 
-    // all jobs of bucket L for variant v (+ copy jobs if `with_copies`)
+    // all jobs of bucket L for variant v (+ copy jobs if `with_copies`);
+    // domain indices are global (scene base + local)
     std::vector<DevJob> make_jobs(int L, const StageVariant* v, bool with_copies) {
         std::vector<DevJob> jobs;
         const int per = 2 * v->CS;
-        for (const StripRun& r : sc.runs) {
-            if (run_length(r) != L) continue;
-            const Domain& d = sc.doms[r.dom];
-            int n = d.len(r.axis);
-            int W = sc.window_for(n);
-            int wo = window_of(W);
-            for (int vel = 0; vel < 2; vel++) {
-                // reflection / transmission of the bands (kernel/core/kernel_functions.cpp:37-64)
-                float rs = d.rho;
-                float r1 = r.d1 >= 0 ? sc.doms[r.d1].rho : rs;
-                float r2 = r.d2 >= 0 ? sc.doms[r.d2].rho : rs;
-                float zn1 = r1 / rs, izn1 = rs / r1, zn2 = r2 / rs, izn2 = rs / r2;
-                float rlw1 = (zn1 - 1) / (zn1 + 1), tlw1 = (2 * zn1) / (zn1 + 1), tlw2 = (2 * izn1) / (izn1 + 1);
-                float rrw1 = (zn2 - 1) / (zn2 + 1), trw1 = (2 * zn2) / (zn2 + 1), trw2 = (2 * izn2) / (izn2 + 1);
-                DevJob j;
-                std::memset(&j, 0, sizeof j);
-                j.dom = r.dom;
-                j.kind = (vel ? JK_VEL : 0) | (r.axis == AX_Y ? JK_Y : 0);
-                j.W = W;
-                j.d1 = r.d1;
-                j.d2 = r.d2;
-                if (vel) { j.R1 = -rlw1; j.T1 = tlw1; j.R2 = -rrw1; j.T2 = trw1; }
-                else     { j.R1 = rlw1;  j.T1 = tlw2; j.R2 = rrw1;  j.T2 = trw2; }
-                j.dtab = filter_of(L, vel, v);
-                j.wtab = wo;
-                int s = r.first, end = r.first + r.count;
-                int origin = d.lo(r.axis);
-                while (s < end) {
-                    int e = std::min(end, (s / per + 1) * per);   // cut at multiples of `per`
-                    j.first = s;
-                    j.count = e - s;
-                    j.o1 = r.d1 >= 0 ? origin + s - sc.doms[r.d1].lo(r.axis) : 0;
-                    j.o2 = r.d2 >= 0 ? origin + s - sc.doms[r.d2].lo(r.axis) : 0;
-                    jobs.push_back(j);
-                    s = e;
+        for (size_t si = 0; si < scenes.size(); si++) {
+            const Scene& sc = scenes[si];
+            const int base = dom_base[si];
+            for (const StripRun& r : sc.runs) {
+                if (run_length(sc, r) != L) continue;
+                const Domain& d = sc.doms[r.dom];
+                int n = d.len(r.axis);
+                int W = sc.window_for(n);
+                int wo = window_of(W, (int)sc.s.patcherror);
+                for (int vel = 0; vel < 2; vel++) {
+                    // reflection / transmission of the bands (kernel/core/kernel_functions.cpp:37-64)
+                    float rs = d.rho;
+                    float r1 = r.d1 >= 0 ? sc.doms[r.d1].rho : rs;
+                    float r2 = r.d2 >= 0 ? sc.doms[r.d2].rho : rs;
+                    float zn1 = r1 / rs, izn1 = rs / r1, zn2 = r2 / rs, izn2 = rs / r2;
+                    float rlw1 = (zn1 - 1) / (zn1 + 1), tlw1 = (2 * zn1) / (zn1 + 1), tlw2 = (2 * izn1) / (izn1 + 1);
+                    float rrw1 = (zn2 - 1) / (zn2 + 1), trw1 = (2 * zn2) / (zn2 + 1), trw2 = (2 * izn2) / (izn2 + 1);
+                    DevJob j;
+                    std::memset(&j, 0, sizeof j);
+                    j.dom = base + r.dom;
+                    j.kind = (vel ? JK_VEL : 0) | (r.axis == AX_Y ? JK_Y : 0);
+                    j.W = W;
+                    j.d1 = r.d1 >= 0 ? base + r.d1 : -1;
+                    j.d2 = r.d2 >= 0 ? base + r.d2 : -1;
+                    if (vel) { j.R1 = -rlw1; j.T1 = tlw1; j.R2 = -rrw1; j.T2 = trw1; }
+                    else     { j.R1 = rlw1;  j.T1 = tlw2; j.R2 = rrw1;  j.T2 = trw2; }
+                    j.dtab = filter_of(L, vel, v, sc.s.dx);
+                    j.wtab = wo;
+                    int s_ = r.first, end = r.first + r.count;
+                    int origin = d.lo(r.axis);
+                    while (s_ < end) {
+                        int e = std::min(end, (s_ / per + 1) * per);   // cut at multiples of `per`
+                        j.first = s_;
+                        j.count = e - s_;
+                        j.o1 = r.d1 >= 0 ? origin + s_ - sc.doms[r.d1].lo(r.axis) : 0;
+                        j.o2 = r.d2 >= 0 ? origin + s_ - sc.doms[r.d2].lo(r.axis) : 0;
+                        jobs.push_back(j);
+                        s_ = e;
+                    }
                 }
             }
         }
         if (with_copies) {
-            for (size_t k = 0; k < sc.doms.size(); k++) {
-                const Domain& d = sc.doms[k];
+            for (size_t g = 0; g < gdom.size(); g++) {
+                const Domain& d = dom((int)g);
                 if (d.rigid) continue;
                 for (int ax = 0; ax < 2; ax++) {
                     if (d.update[ax]) continue;
                     DevJob j;
                     std::memset(&j, 0, sizeof j);
-                    j.dom = (int)k;
+                    j.dom = (int)g;
                     j.kind = JK_COPY | (ax == AX_Y ? JK_Y : 0);
                     j.d1 = j.d2 = -1;
                     jobs.push_back(j);
@@ -302,9 +314,31 @@ struct Kernel {
     }
 
     // ---------------------------------------------------------------- build
-    void build(const pstd_config* cfg) {
-        sc.build(cfg);
-        framecount = sc.s.framecount();
+    void build(const pstd_config* cfgs, int n_cfg) {
+        build_scenes(cfgs, n_cfg);
+        build_device();
+    }
+
+    void build_scenes(const pstd_config* cfgs, int n_cfg) {
+        if (n_cfg <= 0) throw SceneError(PSTD_ERR_INVALID, "no scenes");
+        scenes.resize(n_cfg);
+        for (int i = 0; i < n_cfg; i++) {
+            try {
+                scenes[i].build(&cfgs[i]);
+            } catch (SceneError& e) {
+                if (n_cfg == 1) throw;
+                throw SceneError(e.code, "scene " + std::to_string(i) + ": " + e.what());
+            }
+            dom_base.push_back((int)gdom.size());
+            for (size_t k = 0; k < scenes[i].doms.size(); k++) gdom.push_back({i, (int)k});
+        }
+        int nr = 0;
+        for (auto& sc : scenes) { rec_base.push_back(nr); nr += (int)sc.receivers.size(); }
+        framecount = 0;
+        for (auto& sc : scenes) framecount = std::max(framecount, sc.s.framecount());
+    }
+
+    void build_device() {
         if (const char* e = std::getenv("PSTD_AUTOTUNE")) autotune = std::atoi(e) != 0;
         // PSTD_VARIANT=i pins every bucket to its i-th compiled variant (tests)
         int forced = -1;
@@ -315,11 +349,12 @@ struct Kernel {
         // ---- layout
         auto round32 = [](long long v) { return (v + 31) / 32 * 32; };
         long long off = 0, foff = 0, poff = 0;
-        hdoms.resize(sc.doms.size());
+        hdoms.resize(gdom.size());
         std::vector<float> att;
         std::vector<int> pml_idx;
-        for (size_t k = 0; k < sc.doms.size(); k++) {
-            const Domain& d = sc.doms[k];
+        for (size_t k = 0; k < gdom.size(); k++) {
+            const Domain& d = dom((int)k);
+            const Scene& sc = scene_of((int)k);
             DevDomain& h = hdoms[k];
             std::memset(&h, 0, sizeof h);
             h.nx = d.nx; h.ny = d.ny;
@@ -327,6 +362,7 @@ struct Kernel {
             h.pitch_vx = (int)round32(d.nx + 1);
             h.pitch_vy = (int)round32(d.nx);
             h.fixed = d.rigid;
+            h.scene = gdom[k].first;
             long long& o = d.rigid ? foff : off;
             h.o_px = o; o = round32(o + (long long)h.pitch_p * d.ny);
             h.o_py = o; o = round32(o + (long long)h.pitch_p * d.ny);
@@ -369,10 +405,11 @@ struct Kernel {
 
         // ---- buckets
         std::vector<int> Ls;
-        for (const StripRun& r : sc.runs) {
-            int L = run_length(r);
-            if (std::find(Ls.begin(), Ls.end(), L) == Ls.end()) Ls.push_back(L);
-        }
+        for (auto& sc : scenes)
+            for (const StripRun& r : sc.runs) {
+                int L = run_length(sc, r);
+                if (std::find(Ls.begin(), Ls.end(), L) == Ls.end()) Ls.push_back(L);
+            }
         std::sort(Ls.begin(), Ls.end());
         for (int L : Ls) {
             const StageVariant* vs;
@@ -395,39 +432,45 @@ struct Kernel {
         init_fixed.alloc(fixed_floats);
         p0.alloc(p0_floats);
         init_p0.alloc(p0_floats);
-        first_step.alloc(1);
+        first_step.alloc(scenes.size());
         CK(cudaMemsetAsync(init_set.p, 0, set_floats * sizeof(float), stream));
         CK(cudaMemsetAsync(init_fixed.p, 0, fixed_floats * sizeof(float), stream));
         CK(cudaMemsetAsync(init_p0.p, 0, p0_floats * sizeof(float), stream));
-        if (!sc.speakers.empty()) {
+        {
             std::vector<int> x0, y0;
-            for (auto& d : sc.doms) { x0.push_back(d.x0); y0.push_back(d.y0); }
+            for (size_t g = 0; g < gdom.size(); g++) { x0.push_back(dom((int)g).x0); y0.push_back(dom((int)g).y0); }
             DevBuf<int> dx0, dy0;
             dx0.upload(x0);
             dy0.upload(y0);
-            std::vector<DevSpeaker> spk;
-            for (auto& s : sc.speakers) spk.push_back({s.x, s.y});
-            DevBuf<DevSpeaker> dspk;
-            dspk.upload(spk);
-            CK(launch_speakers(ddoms.p, dx0.p, dy0.p, (int)sc.doms.size(), dspk.p, (int)spk.size(), sc.s.dx,
-                               sc.s.band_width, init_set.p, init_fixed.p, init_p0.p, stream));
-            CK(cudaStreamSynchronize(stream));
+            for (size_t si = 0; si < scenes.size(); si++) {
+                const Scene& sc = scenes[si];
+                if (sc.speakers.empty()) continue;
+                std::vector<DevSpeaker> spk;
+                for (auto& q : sc.speakers) spk.push_back({q.x, q.y});
+                DevBuf<DevSpeaker> dspk;
+                dspk.upload(spk);
+                const int b = dom_base[si];
+                CK(launch_speakers(ddoms.p + b, dx0.p + b, dy0.p + b, (int)sc.doms.size(), dspk.p, (int)spk.size(),
+                                   sc.s.dx, sc.s.band_width, init_set.p, init_fixed.p, init_p0.p, stream));
+                CK(cudaStreamSynchronize(stream));
+            }
         }
 
         // ---- receivers, frames
         std::vector<DevReceiver> rec;
-        for (auto& r : sc.receivers) rec.push_back({r.dom, r.row, r.col});
+        for (size_t si = 0; si < scenes.size(); si++)
+            for (auto& r : scenes[si].receivers) rec.push_back({dom_base[si] + r.dom, r.row, r.col});
         n_rec = (int)rec.size();
         drec.upload(rec);
         ring_cap = std::max(framecount, 1);
         dring.alloc((size_t)ring_cap * std::max(n_rec, 1));
         dcounter.alloc(1);
         frame_floats = 0;
-        for (size_t k = 0; k < sc.doms.size(); k++) {
-            if (sc.doms[k].pml) continue;
+        for (size_t k = 0; k < gdom.size(); k++) {
+            if (dom((int)k).pml) continue;
             frame_doms.push_back((int)k);
             frame_off.push_back((long long)frame_floats);
-            frame_floats += (size_t)sc.doms[k].nx * sc.doms[k].ny;
+            frame_floats += (size_t)dom((int)k).nx * dom((int)k).ny;
         }
         dframe_doms.upload(frame_doms);
         dframe_off.upload(frame_off);
@@ -445,8 +488,8 @@ struct Kernel {
         capture_graphs();
         std::string choice;
         for (auto& b : buckets) choice += " [" + std::string(b.var->name) + b.choice + "]";
-        log(PSTD_LOG_DEBUG, "scene: " + std::to_string(sc.doms.size()) + " domains, " + std::to_string(sc.speakers.size()) +
-                                " speakers, " + std::to_string(sc.receivers.size()) + " receivers; stage kernels:" + choice);
+        log(PSTD_LOG_DEBUG, std::to_string(scenes.size()) + " scene(s), " + std::to_string(gdom.size()) + " domains, " +
+                                std::to_string(n_rec) + " receivers; stage kernels:" + choice);
     }
 
     StageArgs stage_args(int c, int k, const DevJob* jobs, const float2* twp, int fp = 0, int fv = 0) {
@@ -477,7 +520,14 @@ struct Kernel {
         dwin.upload(win);
     }
 
-    // choose a variant per bucket by timing each on this scene's jobs
+    // the persistent form stages one pressure / velocity filter pair per CTA
+    static bool one_filter_pair(const std::vector<DevJob>& jobs, int fp, int fv) {
+        for (const DevJob& j : jobs)
+            if (!(j.kind & JK_COPY) && j.dtab != ((j.kind & JK_VEL) ? fv : fp)) return false;
+        return true;
+    }
+
+    // choose a variant per bucket by timing each on this batch's jobs
     void plan(bool tune) {
         if (tune) {
             for (auto& b : buckets) {
@@ -489,8 +539,9 @@ struct Kernel {
                 for (int i = 0; i < nv; i++) {
                     all[i] = make_jobs(b.L, &vs[i], false);
                     twv[i] = twiddles_of(&vs[i]);
-                    fpv[i] = filter_of(b.L, false, &vs[i]);
-                    fvv[i] = filter_of(b.L, true, &vs[i]);
+                    fpv[i] = filter_of(b.L, false, &vs[i], scenes[0].s.dx);
+                    fvv[i] = filter_of(b.L, true, &vs[i], scenes[0].s.dx);
+                    if (vs[i].persistent && !one_filter_pair(all[i], fpv[i], fvv[i])) all[i].clear();
                 }
                 upload_tables();
                 float best = 1e30f;
@@ -529,8 +580,17 @@ struct Kernel {
             auto& b = buckets[i];
             auto js = make_jobs(b.L, b.var, i + 1 == buckets.size());
             b.tw_off = twiddles_of(b.var);
-            b.fp_off = filter_of(b.L, false, b.var);
-            b.fv_off = filter_of(b.L, true, b.var);
+            b.fp_off = filter_of(b.L, false, b.var, scenes[0].s.dx);
+            b.fv_off = filter_of(b.L, true, b.var, scenes[0].s.dx);
+            if (b.var->persistent && !one_filter_pair(js, b.fp_off, b.fv_off)) {
+                // mixed grid spacings: fall back to the first plain variant
+                const StageVariant* vs;
+                int nv = stage_variants(b.L, &vs);
+                for (int q = 0; q < nv; q++) if (!vs[q].persistent) { b.var = &vs[q]; break; }
+                js = make_jobs(b.L, b.var, i + 1 == buckets.size());
+                b.tw_off = twiddles_of(b.var);
+                b.choice += " (plain: several grid spacings)";
+            }
             b.off = (int)jobs.size();
             b.n = (int)js.size();
             jobs.insert(jobs.end(), js.begin(), js.end());
@@ -544,8 +604,8 @@ struct Kernel {
         CK(cudaMemcpyAsync(sets[0].p, init_set.p, set_floats * sizeof(float), cudaMemcpyDeviceToDevice, stream));
         CK(cudaMemcpyAsync(fixed.p, init_fixed.p, fixed_floats * sizeof(float), cudaMemcpyDeviceToDevice, stream));
         CK(cudaMemcpyAsync(p0.p, init_p0.p, p0_floats * sizeof(float), cudaMemcpyDeviceToDevice, stream));
-        const int one = 1;
-        CK(cudaMemcpyAsync(first_step.p, &one, sizeof(int), cudaMemcpyHostToDevice, stream));
+        std::vector<int> ones(scenes.size(), 1);
+        CK(cudaMemcpy(first_step.p, ones.data(), ones.size() * sizeof(int), cudaMemcpyHostToDevice));
         CK(cudaMemsetAsync(dcounter.p, 0, sizeof(int), stream));
         CK(cudaStreamSynchronize(stream));
         cur = 0;
@@ -602,8 +662,8 @@ struct Kernel {
                 ev->push_back({t0, t1});
             }
         }
-        if (n_pml > 0) CK(launch_pml_post(dpml.p, n_pml, ddoms.p, sets[B].p, fixed.p, p0.p, datt.p, first_step.p, st));
-        else CK(cudaMemsetAsync(first_step.p, 0, sizeof(int), st));
+        if (n_pml > 0) CK(launch_pml_post(dpml.p, n_pml, ddoms.p, sets[B].p, fixed.p, p0.p, datt.p, st));
+        CK(cudaMemsetAsync(first_step.p, 0, scenes.size() * sizeof(int), st));
         CK(launch_receivers(drec.p, n_rec, ddoms.p, sets[B].p, dring.p, ring_cap, dcounter.p, st));
         for (auto e : tmp) cudaEventDestroy(e);   // destruction is deferred until the event completes
     }
@@ -640,8 +700,10 @@ struct Kernel {
 };
 
 static int run_frames(Kernel* k, const pstd_callbacks* cb) {
+    if (k->scenes.size() != 1) throw SceneError(PSTD_ERR_INVALID, "run() delivers frames of a single scene; advance batches");
+    const Scene& sc = k->scenes[0];
     const int nframes = k->framecount;
-    const int save = std::max(1, k->sc.s.save_nth);
+    const int save = std::max(1, sc.s.save_nth);
     const size_t frame_floats = k->frame_floats;
     const int K = 3;   // frames in flight
     const size_t slot = frame_floats + (size_t)std::max(k->n_rec, 1);
@@ -660,18 +722,18 @@ static int run_frames(Kernel* k, const pstd_callbacks* cb) {
             int d = k->frame_doms[i];
             size_t n = (size_t)k->hdoms[d].nx * k->hdoms[d].ny;
             if (cb && cb->write_frame && status == PSTD_OK)
-                if (cb->write_frame(cb->user, p.frame, k->sc.doms[d].id, base + k->frame_off[i], (int64_t)n) != 0)
+                if (cb->write_frame(cb->user, p.frame, sc.doms[d].id, base + k->frame_off[i], (int64_t)n) != 0)
                     status = PSTD_ERR_CALLBACK;
         }
         for (int r = 0; r < k->n_rec; r++) {
             if (cb && cb->write_sample && status == PSTD_OK)
-                if (cb->write_sample(cb->user, p.frame, k->sc.receivers[r].id, base + frame_floats + r, 1) != 0)
+                if (cb->write_sample(cb->user, p.frame, sc.receivers[r].id, base + frame_floats + r, 1) != 0)
                     status = PSTD_ERR_CALLBACK;
         }
         log(PSTD_LOG_INFO, "Finished frame: " + std::to_string(p.frame));
     };
-    log(PSTD_LOG_DEBUG, "Number of render time: " + std::to_string(k->sc.s.calctime));
-    log(PSTD_LOG_DEBUG, "Size of time step: " + std::to_string(k->sc.s.dt()));
+    log(PSTD_LOG_DEBUG, "Number of render time: " + std::to_string(sc.s.calctime));
+    log(PSTD_LOG_DEBUG, "Size of time step: " + std::to_string(sc.s.dt()));
     log(PSTD_LOG_INFO, "Starting simulation");
     int next_slot = 0;
     for (int f = 0; f < nframes && status == PSTD_OK; f++) {
@@ -753,7 +815,7 @@ int pstd_create(const pstd_config* config, const pstd_callbacks* log_cb, pstd_ke
         h->k = std::make_unique<Kernel>();
         if (log_cb) { h->k->logcb = *log_cb; h->k->have_logcb = true; }
         h->k->log(PSTD_LOG_DEBUG, "Initializing kernel");
-        h->k->build(config);
+        h->k->build(config, 1);
         h->k->log(PSTD_LOG_DEBUG, "Finished initializing kernel");
         *out = h.release();
         return PSTD_OK;
@@ -766,12 +828,44 @@ int pstd_scene_build(const pstd_config* config, pstd_kernel** out) {
     GUARD({
         auto h = std::make_unique<pstd_kernel>();
         h->k = std::make_unique<Kernel>();
-        h->k->sc.build(config);
-        h->k->framecount = h->k->sc.s.framecount();
+        h->k->build_scenes(config, 1);
         h->k->host_only = true;
         *out = h.release();
         return PSTD_OK;
     })
+}
+
+int pstd_create_batch(const pstd_config* configs, int32_t n, const pstd_callbacks* log_cb, pstd_kernel** out) {
+    if (!out) return fail(PSTD_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    if (!configs || n <= 0) return fail(PSTD_ERR_INVALID, "empty batch");
+    GUARD({
+        auto h = std::make_unique<pstd_kernel>();
+        h->k = std::make_unique<Kernel>();
+        if (log_cb) { h->k->logcb = *log_cb; h->k->have_logcb = true; }
+        h->k->build(configs, n);
+        *out = h.release();
+        return PSTD_OK;
+    })
+}
+
+int pstd_batch_scene(pstd_kernel* h, int32_t scene, int32_t* info) {
+    NEED(h);
+    auto* k = h->k.get();
+    if (scene < 0 || scene >= (int)k->scenes.size()) return fail(PSTD_ERR_INVALID, "scene index out of range");
+    info[0] = k->dom_base[scene];
+    info[1] = (int32_t)k->scenes[scene].doms.size();
+    info[2] = k->rec_base[scene];
+    info[3] = (int32_t)k->scenes[scene].receivers.size();
+    info[4] = k->scenes[scene].s.framecount();
+    return PSTD_OK;
+}
+
+int pstd_batch_size(pstd_kernel* h, int32_t* n_scenes, int32_t* n_receivers) {
+    NEED(h);
+    if (n_scenes) *n_scenes = (int32_t)h->k->scenes.size();
+    if (n_receivers) *n_receivers = h->k->n_rec;
+    return PSTD_OK;
 }
 
 void pstd_destroy(pstd_kernel* k) {
@@ -781,11 +875,11 @@ void pstd_destroy(pstd_kernel* k) {
 
 int pstd_get_metadata(pstd_kernel* h, int32_t* n_domains, int32_t* dims, int32_t cap, int32_t* framecount) {
     NEED(h);
-    auto& sc = h->k->sc;
-    if (n_domains) *n_domains = (int32_t)sc.doms.size();
-    for (int i = 0; i < (int)sc.doms.size() && i < cap && dims; i++) {
-        dims[3 * i] = sc.doms[i].nx;
-        dims[3 * i + 1] = sc.doms[i].ny;
+    auto* k = h->k.get();
+    if (n_domains) *n_domains = (int32_t)k->gdom.size();
+    for (int i = 0; i < (int)k->gdom.size() && i < cap && dims; i++) {
+        dims[3 * i] = k->dom(i).nx;
+        dims[3 * i + 1] = k->dom(i).ny;
         dims[3 * i + 2] = 0;
     }
     if (framecount) *framecount = h->k->framecount;
@@ -891,12 +985,16 @@ int pstd_snapshot(pstd_kernel* h, int32_t idx, int32_t field, float* dst, int64_
 
 int pstd_scene_strip_runs(pstd_kernel* h, int32_t idx, int32_t axis, int32_t* runs, int32_t cap, int32_t* n) {
     NEED(h);
-    auto& sc = h->k->sc;
+    auto* k = h->k.get();
+    if (idx < 0 || idx >= (int)k->gdom.size()) return fail(PSTD_ERR_INVALID, "domain index out of range");
+    const Scene& sc = k->scene_of(idx);
+    const int base = k->dom_base[k->gdom[idx].first], local = k->gdom[idx].second;
     int c = 0;
     for (const StripRun& r : sc.runs) {
-        if (r.dom != idx || (int)r.axis != axis) continue;
+        if (r.dom != local || (int)r.axis != axis) continue;
         if (c < cap && runs) {
-            runs[4 * c] = r.first; runs[4 * c + 1] = r.count; runs[4 * c + 2] = r.d1; runs[4 * c + 3] = r.d2;
+            runs[4 * c] = r.first; runs[4 * c + 1] = r.count;
+            runs[4 * c + 2] = r.d1 >= 0 ? base + r.d1 : -1; runs[4 * c + 3] = r.d2 >= 0 ? base + r.d2 : -1;
         }
         c++;
     }
@@ -906,15 +1004,16 @@ int pstd_scene_strip_runs(pstd_kernel* h, int32_t idx, int32_t axis, int32_t* ru
 
 int pstd_scene_domain_count(pstd_kernel* h, int32_t* n) {
     NEED(h);
-    *n = (int32_t)h->k->sc.doms.size();
+    *n = (int32_t)h->k->gdom.size();
     return PSTD_OK;
 }
 
 int pstd_scene_domain_info(pstd_kernel* h, int32_t idx, pstd_domain_info* o) {
     NEED(h);
-    auto& sc = h->k->sc;
-    if (idx < 0 || idx >= (int)sc.doms.size()) return fail(PSTD_ERR_INVALID, "domain index out of range");
-    const Domain& d = sc.doms[idx];
+    auto* k = h->k.get();
+    if (idx < 0 || idx >= (int)k->gdom.size()) return fail(PSTD_ERR_INVALID, "domain index out of range");
+    const Scene& sc = k->scene_of(idx);
+    const Domain& d = k->dom(idx);
     std::memset(o, 0, sizeof *o);
     o->id = d.id;
     o->top_left[0] = d.x0; o->top_left[1] = d.y0;
@@ -934,19 +1033,21 @@ int pstd_scene_domain_info(pstd_kernel* h, int32_t idx, pstd_domain_info* o) {
 
 int pstd_scene_neighbours(pstd_kernel* h, int32_t idx, int32_t dir, int32_t* out, int32_t cap, int32_t* n) {
     NEED(h);
-    auto& sc = h->k->sc;
-    if (idx < 0 || idx >= (int)sc.doms.size() || dir < 0 || dir > 3) return fail(PSTD_ERR_INVALID, "bad index or side");
-    const auto& v = sc.doms[idx].nb[dir];
+    auto* k = h->k.get();
+    if (idx < 0 || idx >= (int)k->gdom.size() || dir < 0 || dir > 3) return fail(PSTD_ERR_INVALID, "bad index or side");
+    const auto& v = k->dom(idx).nb[dir];
+    const int base = k->dom_base[k->gdom[idx].first];
     *n = (int32_t)v.size();
-    for (int i = 0; i < (int)v.size() && i < cap; i++) out[i] = v[i];
+    for (int i = 0; i < (int)v.size() && i < cap; i++) out[i] = base + v[i];
     return PSTD_OK;
 }
 
 int pstd_scene_attenuation(pstd_kernel* h, int32_t idx, float* ax_p, float* ax_v, float* ay_p, float* ay_v) {
     NEED(h);
-    auto& sc = h->k->sc;
-    if (idx < 0 || idx >= (int)sc.doms.size()) return fail(PSTD_ERR_INVALID, "domain index out of range");
-    const Domain& d = sc.doms[idx];
+    auto* k = h->k.get();
+    if (idx < 0 || idx >= (int)k->gdom.size()) return fail(PSTD_ERR_INVALID, "domain index out of range");
+    const Scene& sc = k->scene_of(idx);
+    const Domain& d = k->dom(idx);
     std::vector<double> prof;
     auto fill = [&](float* dst, int n, bool on, bool vel, bool asc) {
         if (!dst) return;

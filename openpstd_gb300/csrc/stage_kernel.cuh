@@ -577,7 +577,7 @@ __global__ void __launch_bounds__(C::NT, C::MINB) stage_kernel(StageArgs A) {
         copy_axis<C::NT>(A, dom, job.kind & JK_Y, threadIdx.x);
         return;
     }
-    const bool first = *A.first_step != 0;
+    const bool first = A.first_step[dom.scene] != 0;
     gather<C, C::NT>(sm, A, job, dom, first, threadIdx.x);
     __syncthreads();
     convolve<C, C::NT, 0, false>(sm, A.tw, A.filt + job.dtab, threadIdx.x);
@@ -624,12 +624,12 @@ __global__ void __launch_bounds__(C::NT + C::NTP, 1) stage_ws(StageArgs A, int n
         // memory warps: gather job k while the FFT warps transform job k-1,
         // then write back job k-1
         const int ptid = tid - NTC;
-        const bool first = *A.first_step != 0;
         for (int k = 0; k <= mine; k++) {
             if (k < mine) {
                 const int b = k & 1;
                 const DevJob job = A.jobs[blockIdx.x + k * stride];
-                if (!(job.kind & JK_COPY)) gather<C, NTP>(sm + b * C::BUF, A, job, A.doms[job.dom], first, ptid);
+                const DevDomain dom = A.doms[job.dom];
+                if (!(job.kind & JK_COPY)) gather<C, NTP>(sm + b * C::BUF, A, job, dom, A.first_step[dom.scene] != 0, ptid);
                 bar_arrive(1 + b, ALL);
             }
             if (k >= 1) {
