@@ -504,6 +504,13 @@ __device__ __forceinline__ void gather(float2* sm, const StageArgs& A, const Dev
 }
 
 // ---- step 5: slice, RK update, (sixth stage) PML on vx / vy
+// RK update of one value in the reference's operation order
+// (kernel/Solver.cpp:174-181): v0 - (dt*a_k) * (L / rho) and p0 - (dt*a_k) * ((L*rho)*c^2)
+__device__ __forceinline__ float rk_update(float prev, float d, bool vel, float cdt, float rho, float c2) {
+    return vel ? __fsub_rn(prev, __fmul_rn(cdt, __fmul_rn(__fmul_rn(d, rho), c2)))
+               : __fsub_rn(prev, __fmul_rn(cdt, __fdiv_rn(d, rho)));
+}
+
 template <class C, int NTH>
 __device__ __forceinline__ void epilogue(const float2* sm, const StageArgs& A, const DevJob& job, const DevDomain& dom,
                                          int tid) {
@@ -512,6 +519,8 @@ __device__ __forceinline__ void epilogue(const float2* sm, const StageArgs& A, c
     constexpr int WPP = NW >= CS ? NW / CS : 1;
     constexpr int PST = NW / WPP;
     const float* smf = reinterpret_cast<const float*>(sm);
+    const float* __restrict__ prev = A.prev;
+    float* __restrict__ out = A.out;
     const int warp = tid >> 5, lane = tid & 31;
     const bool vel = job.kind & JK_VEL;
     const bool ydir = job.kind & JK_Y;
@@ -528,41 +537,73 @@ __device__ __forceinline__ void epilogue(const float2* sm, const StageArgs& A, c
     else { fo = ydir ? dom.o_py : dom.o_px; fp = dom.pitch_p; ao = -1; }
     const bool att = A.last && ao >= 0;
     if (!ydir) {
+        // rows: four consecutive outputs per lane (16-byte loads / stores), two chunks in flight
+        const int chunks = (nout + 3) >> 2;
         for (int cs = warp / WPP; cs < CS; cs += PST) {
             const float2* srow = sm + cs * SP + W;
-            for (int i = (warp % WPP) * 32 + lane; i < nout; i += WPP * 32) {
-                const float2 d = srow[i];
+            const long long r0 = fo + (long long)(job.first + 2 * cs) * fp;
+            const bool h1 = 2 * cs + 1 < count;
+            if (2 * cs >= count) continue;
+            for (int c0 = (warp % WPP) * 32 + lane; c0 < chunks; c0 += 2 * WPP * 32) {
+                float4 p[2][2];
 #pragma unroll
-                for (int h = 0; h < 2; h++) {
-                    const int s = 2 * cs + h;
-                    if (s >= count) break;
-                    const float dv = h ? d.y : d.x;
-                    const long long e = fo + (long long)(job.first + s) * fp + i;
-                    float v;
-                    if (!vel) {
-                        v = __fsub_rn(A.prev[e], __fmul_rn(cdt, __fdiv_rn(dv, rho)));
-                        if (att) v = __fmul_rn(v, A.att[ao + i]);
-                    } else {
-                        v = __fsub_rn(A.prev[e], __fmul_rn(cdt, __fmul_rn(__fmul_rn(dv, rho), c2)));
+                for (int q = 0; q < 2; q++) {
+                    const int i = (c0 + q * WPP * 32) << 2;
+                    p[q][0] = p[q][1] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (i < nout) {
+                        p[q][0] = ld4(prev + r0, i, nout);
+                        if (h1) p[q][1] = ld4(prev + r0 + fp, i, nout);
                     }
-                    A.out[e] = v;
+                }
+#pragma unroll
+                for (int q = 0; q < 2; q++) {
+                    const int i = (c0 + q * WPP * 32) << 2;
+                    if (i >= nout) continue;
+                    float2 d[4];
+#pragma unroll
+                    for (int e = 0; e < 4; e++) d[e] = (i + e < nout) ? srow[i + e] : make_float2(0.f, 0.f);
+#pragma unroll
+                    for (int h = 0; h < 2; h++) {
+                        if (h == 1 && !h1) break;
+                        float v[4] = {p[q][h].x, p[q][h].y, p[q][h].z, p[q][h].w};
+#pragma unroll
+                        for (int e = 0; e < 4; e++) {
+                            v[e] = rk_update(v[e], h ? d[e].y : d[e].x, vel, cdt, rho, c2);
+                            if (att && i + e < nout) v[e] = __fmul_rn(v[e], A.att[ao + i + e]);
+                        }
+                        float* o = out + r0 + (h ? fp : 0) + i;
+                        if (i + 4 <= nout) {
+                            *reinterpret_cast<float4*>(o) = make_float4(v[0], v[1], v[2], v[3]);
+                        } else {
+#pragma unroll
+                            for (int e = 0; e < 4; e++)
+                                if (i + e < nout) o[e] = v[e];
+                        }
+                    }
                 }
             }
         }
     } else {
-        for (int f = tid; f < S2 * nout; f += NTH) {
-            const int s = f % S2, i = f / S2;
-            if (s >= count) continue;
-            const float dv = smf[2 * ((s >> 1) * SP + W + i) + (s & 1)];
-            const long long e = fo + (long long)i * fp + job.first + s;
-            float v;
-            if (!vel) {
-                v = __fsub_rn(A.prev[e], __fmul_rn(cdt, __fdiv_rn(dv, rho)));
-                if (att) v = __fmul_rn(v, A.att[ao + i]);
-            } else {
-                v = __fsub_rn(A.prev[e], __fmul_rn(cdt, __fmul_rn(__fmul_rn(dv, rho), c2)));
+        // columns: consecutive threads on consecutive columns, four values in flight
+        const int total = S2 * nout;
+        for (int f0 = tid; f0 < total; f0 += 4 * NTH) {
+            float pv[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int f = f0 + q * NTH;
+                const int s = f % S2, i = f / S2;
+                pv[q] = (f < total && s < count) ? prev[fo + (long long)i * fp + job.first + s] : 0.f;
             }
-            A.out[e] = v;
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int f = f0 + q * NTH;
+                const int s = f % S2, i = f / S2;
+                if (f >= total || s >= count) continue;
+                const float dv = smf[2 * ((s >> 1) * SP + W + i) + (s & 1)];
+                float v = rk_update(pv[q], dv, vel, cdt, rho, c2);
+                if (att) v = __fmul_rn(v, A.att[ao + i]);
+                out[fo + (long long)i * fp + job.first + s] = v;
+            }
         }
     }
 }
