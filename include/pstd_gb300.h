@@ -220,6 +220,39 @@ int pstd_plan_info(pstd_kernel* k, char* buf, int32_t cap);
  * per time step. */
 int pstd_work_counts(pstd_kernel* k, int64_t* cells, int64_t* air_cells, int32_t* launches_per_step);
 
+/* ---- allocation-free solve (no counterpart in the reference) ------------
+ * For callers that cannot allocate device memory: host applications that
+ * own the GPU's memory through their own pool or arena (a serving process
+ * whose caching allocator has reserved the HBM, an engine with a fixed
+ * device-memory budget) and real-time loops, for which cudaMalloc / cudaFree
+ * may fail under the host's budget and synchronise the device.
+ *
+ * Builds `config` on the host, advances n_steps (>= 1) time steps from the
+ * speaker initial condition on `stream` (a cudaStream_t, NULL = the legacy
+ * default stream) and writes, when the pointers are not NULL:
+ *   frame_dev      p0 after the last step of every non-PML domain, in scene
+ *                  order, each Nx*Ny row-major -- the values pstd_run hands
+ *                  write_frame for that frame (frame_len >= their total);
+ *   receivers_dev  n_steps x n_receivers samples, step-major, as
+ *                  pstd_get_receivers returns them (receivers_len >= that).
+ * Both are DEVICE pointers owned by the caller; results are ready when the
+ * stream's work completes.  The call allocates no device memory: state
+ * sets, tables and plan live in one static device array of
+ * PSTD_NOALLOC_SCRATCH_BYTES per device, held from module load until the
+ * process exits.  Scenes that need more are rejected with PSTD_ERR_INVALID
+ * and a message giving the bytes needed (use pstd_create for those).
+ * The first call on a device takes the array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture.  Every call shares the array and clears it
+ * itself; calls whose GPU work overlaps (other streams, other threads on one
+ * device) race on it.  The plan upload is a pageable host-to-device copy,
+ * so the call waits for work already queued on `stream`.  Each strip length
+ * runs the first plain stage-kernel variant compiled for it (no autotuning),
+ * so results match pstd_create + pstd_advance to FP32 rounding. */
+#define PSTD_NOALLOC_SCRATCH_BYTES (16u << 20)
+int pstd_solve_noalloc(const pstd_config* config, int32_t n_steps, float* frame_dev, int64_t frame_len,
+                       float* receivers_dev, int64_t receivers_len, void* stream);
+
 /* ---- library ------------------------------------------------------------ */
 const char* pstd_last_error(void);
 const char* pstd_version(void);

@@ -64,6 +64,7 @@ SIGNATURES = {
     "pstd_profile_passes": (ctypes.c_int, [_vp, _i32, _vp, _P(_f32), _P(_f32), _P(_i32), _P(_i32)]),
     "pstd_plan_info": (ctypes.c_int, [_vp, ctypes.c_char_p, _i32]),
     "pstd_work_counts": (ctypes.c_int, [_vp, _P(_i64), _P(_i64), _P(_i32)]),
+    "pstd_solve_noalloc": (ctypes.c_int, [_P(c_config), _i32, _vp, _i64, _vp, _i64, _vp]),
     "pstd_last_error": (ctypes.c_char_p, []),
     "pstd_version": (ctypes.c_char_p, []),
 }

@@ -22,6 +22,7 @@
 #include <deque>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <tuple>
 #include <vector>
@@ -1120,3 +1121,264 @@ int pstd_plan_info(pstd_kernel* h, char* buf, int32_t cap) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// pstd_solve_noalloc: the solve of pstd_create + pstd_advance + frame output
+// for callers that cannot allocate device memory.  Such callers are host
+// applications that own the GPU's memory through their own pool or arena
+// (a serving process whose caching allocator has reserved the HBM, an
+// acoustics or game engine with a fixed device-memory budget) and real-time
+// loops (auralisation) that cannot take cudaMalloc / cudaFree, which may fail
+// under the host's budget and synchronise the device.  The caller passes the
+// configuration (input) and device buffers for the outputs; everything else
+// the solve needs -- the three rotating state sets (the stage kernels'
+// scratch), the fixed buffer of rigid domains, p0, the step flag, domain
+// table, strip jobs, FP64-derived tables and receiver / speaker lists --
+// lives in one file-scope device array of PSTD_NOALLOC_SCRATCH_BYTES.
+// ---------------------------------------------------------------------------
+namespace pstd {
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[PSTD_NOALLOC_SCRATCH_BYTES];
+
+static std::mutex g_noalloc_mu;
+static constexpr int kNoAllocDevices = 256;
+static unsigned char* g_noalloc_base[kNoAllocDevices] = {};
+
+// Device address of the scratch array on the current device.  In host code
+// `g_noalloc_scratch` is only a stand-in for the symbol; its address on a
+// device comes from cudaGetSymbolAddress, taken once per device (with that
+// device current) at the first call on it.
+static unsigned char* noalloc_scratch() {
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocDevices) throw CudaError("device ordinal out of range for the scratch table");
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_base[dev]) {
+        void* p = nullptr;
+        CK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        g_noalloc_base[dev] = static_cast<unsigned char*>(p);
+    }
+    return g_noalloc_base[dev];
+}
+
+static int solve_noalloc(const pstd_config* config, int n_steps, float* frame_dev, int64_t frame_len, float* rec_dev,
+                         int64_t rec_len, cudaStream_t st) {
+    if (!config) return fail(PSTD_ERR_INVALID, "config is NULL");
+    if (n_steps < 1) return fail(PSTD_ERR_INVALID, "n_steps must be at least 1");
+    if ((frame_len && !frame_dev) || (rec_len && !rec_dev) || frame_len < 0 || rec_len < 0)
+        return fail(PSTD_ERR_INVALID, "output pointer is NULL or its length is negative");
+
+    // host-side scene, tables and strip jobs (no device state: nothing here
+    // allocates device memory)
+    Kernel kh;
+    kh.build_scenes(config, 1);
+    const Scene& sc = kh.scenes[0];
+    const int nd = (int)kh.gdom.size();
+
+    // field layout of pstd_create (device.cuh)
+    auto round32 = [](long long v) { return (v + 31) / 32 * 32; };
+    long long off = 0, foff = 0, poff = 0;
+    std::vector<DevDomain> hd(nd);
+    std::vector<float> att;
+    std::vector<int> pml_idx, x0, y0, frame_doms;
+    std::vector<long long> frame_off;
+    long long frame_floats = 0;
+    for (int k = 0; k < nd; k++) {
+        const Domain& d = kh.dom(k);
+        DevDomain& h = hd[k];
+        std::memset(&h, 0, sizeof h);
+        h.nx = d.nx; h.ny = d.ny;
+        h.pitch_p = (int)round32(d.nx);
+        h.pitch_vx = (int)round32(d.nx + 1);
+        h.pitch_vy = (int)round32(d.nx);
+        h.fixed = d.rigid;
+        h.scene = 0;
+        long long& o = d.rigid ? foff : off;
+        h.o_px = o; o = round32(o + (long long)h.pitch_p * d.ny);
+        h.o_py = o; o = round32(o + (long long)h.pitch_p * d.ny);
+        h.o_vx = o; o = round32(o + (long long)h.pitch_vx * d.ny);
+        h.o_vy = o; o = round32(o + (long long)h.pitch_vy * (d.ny + 1));
+        h.o_p0 = poff; poff = round32(poff + (long long)h.pitch_p * d.ny);
+        h.rho = d.rho;
+        h.c2 = sc.s.c1 * sc.s.c1;
+        const float dt = sc.s.dt();
+        for (int i = 0; i < 6; i++) h.cdt[i] = dt * sc.s.rk[i];
+        h.pml = d.pml;
+        h.att_xp = h.att_xv = h.att_yp = h.att_yv = -1;
+        if (d.pml) {
+            pml_idx.push_back(k);
+            std::vector<double> prof;
+            auto put = [&](bool vel, bool asc, int& at) {
+                pml_profile(sc.s, vel, asc, prof);
+                at = (int)att.size();
+                for (double v : prof) att.push_back((float)v);
+            };
+            if (d.att_x) { put(false, d.asc_x, h.att_xp); put(true, d.asc_x, h.att_xv); }
+            if (d.att_y) { put(false, d.asc_y, h.att_yp); put(true, d.asc_y, h.att_yv); }
+        } else {
+            frame_doms.push_back(k);
+            frame_off.push_back(frame_floats);
+            frame_floats += (long long)d.nx * d.ny;
+        }
+        x0.push_back(d.x0);
+        y0.push_back(d.y0);
+    }
+    if (att.empty()) att.push_back(1.f);
+
+    const int n_rec = (int)sc.receivers.size();
+    if (frame_dev && frame_len < frame_floats)
+        return fail(PSTD_ERR_INVALID, "frame output holds " + std::to_string(frame_len) + " floats; the scene's frame has " +
+                                          std::to_string(frame_floats));
+    if (rec_dev && rec_len < (int64_t)n_steps * n_rec)
+        return fail(PSTD_ERR_INVALID, "receiver output holds " + std::to_string(rec_len) + " floats; " +
+                                          std::to_string(n_steps) + " steps x " + std::to_string(n_rec) +
+                                          " receivers are needed");
+
+    // strip-length buckets, each with the first plain variant compiled for it
+    struct NB { int L; const StageVariant* var; int off, n, tw; };
+    std::vector<NB> nbs;
+    for (const StripRun& r : sc.runs) {
+        const int L = Kernel::run_length(sc, r);
+        bool seen = false;
+        for (auto& b : nbs) seen |= b.L == L;
+        if (!seen) nbs.push_back({L, nullptr, 0, 0, 0});
+    }
+    std::sort(nbs.begin(), nbs.end(), [](const NB& a, const NB& b) { return a.L < b.L; });
+    std::vector<DevJob> jobs;
+    for (size_t i = 0; i < nbs.size(); i++) {
+        NB& b = nbs[i];
+        const StageVariant* vs;
+        const int nv = stage_variants(b.L, &vs);
+        for (int q = 0; q < nv && !b.var; q++) if (!vs[q].persistent) b.var = &vs[q];
+        if (!b.var)
+            return fail(PSTD_ERR_UNSUPPORTED, "strip transform length " + std::to_string(b.L) +
+                                                  " is outside the compiled range 32..8192");
+        auto js = kh.make_jobs(b.L, b.var, i + 1 == nbs.size());
+        b.off = (int)jobs.size();
+        b.n = (int)js.size();
+        b.tw = kh.twiddles_of(b.var);
+        jobs.insert(jobs.end(), js.begin(), js.end());
+    }
+
+    std::vector<DevReceiver> rec;
+    for (auto& r : sc.receivers) rec.push_back({r.dom, r.row, r.col});
+    std::vector<DevSpeaker> spk;
+    for (auto& q : sc.speakers) spk.push_back({q.x, q.y});
+
+    // carve the scratch array: fields first (cleared every call), then the
+    // tables, uploaded every call from one host image
+    size_t at = 0;
+    auto take = [&](size_t bytes) {
+        const size_t o = at;
+        at = (at + bytes + 255) / 256 * 256;
+        return o;
+    };
+    const size_t set_bytes = (size_t)std::max<long long>(off, 32) * sizeof(float);
+    size_t o_set[3];
+    for (auto& o : o_set) o = take(set_bytes);
+    const size_t o_fixed = take((size_t)std::max<long long>(foff, 32) * sizeof(float));
+    const size_t o_p0 = take((size_t)std::max<long long>(poff, 32) * sizeof(float));
+    const size_t o_tab = at;
+    const size_t o_flags = take(2 * sizeof(int));   // first-step flag, receiver step counter
+    const size_t o_doms = take(hd.size() * sizeof(DevDomain));
+    const size_t o_jobs = take(jobs.size() * sizeof(DevJob));
+    const size_t o_filt = take(kh.filt.size() * sizeof(float2));
+    const size_t o_tw = take(kh.tw.size() * sizeof(float2));
+    const size_t o_win = take(kh.win.size() * sizeof(float));
+    const size_t o_att = take(att.size() * sizeof(float));
+    const size_t o_pml = take(pml_idx.size() * sizeof(int));
+    const size_t o_rec = take(rec.size() * sizeof(DevReceiver));
+    const size_t o_fdom = take(frame_doms.size() * sizeof(int));
+    const size_t o_foff = take(frame_off.size() * sizeof(long long));
+    const size_t o_x0 = take(x0.size() * sizeof(int));
+    const size_t o_y0 = take(y0.size() * sizeof(int));
+    const size_t o_spk = take(spk.size() * sizeof(DevSpeaker));
+    if (at > (size_t)PSTD_NOALLOC_SCRATCH_BYTES)
+        return fail(PSTD_ERR_INVALID, "scene needs " + std::to_string(at) + " bytes of scratch; pstd_solve_noalloc holds " +
+                                          std::to_string((size_t)PSTD_NOALLOC_SCRATCH_BYTES) +
+                                          " (PSTD_NOALLOC_SCRATCH_BYTES): use pstd_create for larger scenes");
+
+    std::vector<unsigned char> image(at - o_tab, 0);
+    auto put = [&](size_t o, const void* src, size_t bytes) {
+        if (bytes) std::memcpy(image.data() + (o - o_tab), src, bytes);
+    };
+    const int flags[2] = {1, 0};
+    put(o_flags, flags, sizeof flags);
+    put(o_doms, hd.data(), hd.size() * sizeof(DevDomain));
+    put(o_jobs, jobs.data(), jobs.size() * sizeof(DevJob));
+    put(o_filt, kh.filt.data(), kh.filt.size() * sizeof(float2));
+    put(o_tw, kh.tw.data(), kh.tw.size() * sizeof(float2));
+    put(o_win, kh.win.data(), kh.win.size() * sizeof(float));
+    put(o_att, att.data(), att.size() * sizeof(float));
+    put(o_pml, pml_idx.data(), pml_idx.size() * sizeof(int));
+    put(o_rec, rec.data(), rec.size() * sizeof(DevReceiver));
+    put(o_fdom, frame_doms.data(), frame_doms.size() * sizeof(int));
+    put(o_foff, frame_off.data(), frame_off.size() * sizeof(long long));
+    put(o_x0, x0.data(), x0.size() * sizeof(int));
+    put(o_y0, y0.data(), y0.size() * sizeof(int));
+    put(o_spk, spk.data(), spk.size() * sizeof(DevSpeaker));
+
+    for (const NB& b : nbs) CK(b.var->prepare());
+    unsigned char* base = noalloc_scratch();
+    auto F = [&](size_t o) { return reinterpret_cast<float*>(base + o); };
+    int* first_step = reinterpret_cast<int*>(base + o_flags);
+    int* counter = first_step + 1;
+    const DevDomain* doms = reinterpret_cast<const DevDomain*>(base + o_doms);
+    const DevJob* djobs = reinterpret_cast<const DevJob*>(base + o_jobs);
+    const float2* tw = reinterpret_cast<const float2*>(base + o_tw);
+
+    // the array keeps the previous call's contents: clear the fields, then
+    // upload this call's tables and flags (first step 1, counter 0); a
+    // pageable-source copy returns once the image has been staged
+    CK(cudaMemsetAsync(base, 0, o_tab, st));
+    CK(cudaMemcpyAsync(base + o_tab, image.data(), image.size(), cudaMemcpyHostToDevice, st));
+    if (!spk.empty())
+        CK(launch_speakers(doms, reinterpret_cast<const int*>(base + o_x0), reinterpret_cast<const int*>(base + o_y0),
+                           nd, reinterpret_cast<const DevSpeaker*>(base + o_spk), (int)spk.size(), sc.s.dx,
+                           sc.s.band_width, F(o_set[0]), F(o_fixed), F(o_p0), st));
+
+    int c = 0;
+    for (int s = 0; s < n_steps; s++) {
+        const int A = (c + 1) % 3, B = (c + 2) % 3;
+        for (int k = 0; k < 6; k++) {
+            StageArgs a;
+            a.doms = doms;
+            a.in = F(o_set[k == 0 ? c : ((k - 1) % 2 == 0 ? A : B)]);
+            a.prev = F(o_set[c]);
+            a.out = F(o_set[k % 2 == 0 ? A : B]);
+            a.fixed = F(o_fixed);
+            a.p0 = F(o_p0);
+            a.first_step = first_step;
+            a.filt = a.filt_p = a.filt_v = reinterpret_cast<const float2*>(base + o_filt);
+            a.win = F(o_win);
+            a.att = F(o_att);
+            a.stage = k;
+            a.last = k == 5;
+            for (const NB& b : nbs) {
+                a.jobs = djobs + b.off;
+                a.tw = tw + b.tw;
+                CK(b.var->launch(b.n, a, st));
+            }
+        }
+        if (!pml_idx.empty())
+            CK(launch_pml_post(reinterpret_cast<const int*>(base + o_pml), (int)pml_idx.size(), doms, F(o_set[B]),
+                               F(o_fixed), F(o_p0), F(o_att), st));
+        CK(cudaMemsetAsync(first_step, 0, sizeof(int), st));
+        if (rec_dev && n_rec > 0)
+            CK(launch_receivers(reinterpret_cast<const DevReceiver*>(base + o_rec), n_rec, doms, F(o_set[B]), rec_dev,
+                                n_steps, counter, st));
+        c = B;
+    }
+    if (frame_dev && !frame_doms.empty())
+        CK(launch_frame(reinterpret_cast<const int*>(base + o_fdom), reinterpret_cast<const long long*>(base + o_foff),
+                        (int)frame_doms.size(), doms, F(o_set[c]), frame_dev, st));
+    return PSTD_OK;
+}
+
+}  // namespace pstd
+
+extern "C" int pstd_solve_noalloc(const pstd_config* config, int32_t n_steps, float* frame_dev, int64_t frame_len,
+                                  float* receivers_dev, int64_t receivers_len, void* stream) {
+    GUARD({ return solve_noalloc(config, n_steps, frame_dev, frame_len, receivers_dev, receivers_len,
+                                 (cudaStream_t)stream); })
+}
