@@ -24,6 +24,7 @@ struct StageArgs {
     const float* att;       // PML attenuation profiles
     int stage;              // 0..5
     int last;               // 1 at the sixth stage
+    int row_cap;            // pipelined form: floats staged per strip (>= strip length + 2, multiple of 4)
 };
 
 // One compiled shape of the stage kernel for one transform length.
@@ -31,8 +32,10 @@ struct StageVariant {
     int L, CS, NT, smem, np;
     int r[4];                                                   // radix of each pass
     bool persistent;                                            // warp-specialised persistent form
+    bool pipe;                                                  // pipelined persistent form (cp.async staging)
     cudaError_t (*launch)(int n_jobs, const StageArgs& a, cudaStream_t st);
     cudaError_t (*prepare)();
+    size_t (*smem_for)(int row_cap);                            // dynamic shared memory of one CTA
     const char* name;
 };
 

@@ -105,6 +105,7 @@ struct Bucket {
     int off = 0, n = 0;            // jobs in djobs
     int tw_off = 0;                // float2 offset of the twiddles in dtw
     int fp_off = 0, fv_off = 0;    // float2 offsets of the pressure / velocity filters
+    int rc = 4;                    // floats staged per strip by the pipelined form
     std::string choice;            // autotune record
 };
 
@@ -120,6 +121,7 @@ struct Kernel {
     bool have_logcb = false;
     bool host_only = false;             // built by pstd_scene_build: no device state
     bool autotune = true;
+    int smem_optin = 0;                 // largest dynamic shared memory a CTA may opt in to
 
     // layout
     std::vector<DevDomain> hdoms;
@@ -345,6 +347,7 @@ struct Kernel {
         int forced = -1;
         if (const char* e = std::getenv("PSTD_VARIANT")) { forced = std::atoi(e); autotune = false; }
         CK(cudaGetDevice(&device));
+        CK(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
         CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
 
         // ---- layout
@@ -421,7 +424,13 @@ struct Kernel {
             for (int i = 0; i < nv; i++) CK(vs[i].prepare());
             Bucket b;
             b.L = L;
+            int longest = 0;
+            for (auto& sc : scenes)
+                for (const StripRun& r : sc.runs)
+                    if (run_length(sc, r) == L) longest = std::max(longest, sc.doms[r.dom].len(r.axis));
+            b.rc = (longest + 2 + 3) / 4 * 4;
             b.var = &vs[forced >= 0 ? std::min(forced, nv - 1) : 0];
+            if (b.var->smem_for(b.rc) > (size_t)smem_optin) b.var = &vs[0];   // pinned form does not fit
             if (forced >= 0) b.choice = " pinned";
             buckets.push_back(b);
         }
@@ -493,7 +502,7 @@ struct Kernel {
                                 std::to_string(n_rec) + " receivers; stage kernels:" + choice);
     }
 
-    StageArgs stage_args(int c, int k, const DevJob* jobs, const float2* twp, int fp = 0, int fv = 0) {
+    StageArgs stage_args(int c, int k, const DevJob* jobs, const float2* twp, int fp, int fv, int rc) {
         const int A = (c + 1) % 3, B = (c + 2) % 3;
         StageArgs a;
         a.jobs = jobs;
@@ -512,6 +521,7 @@ struct Kernel {
         a.att = datt.p;
         a.stage = k;
         a.last = k == 5;
+        a.row_cap = rc;
         return a;
     }
 
@@ -543,6 +553,7 @@ struct Kernel {
                     fpv[i] = filter_of(b.L, false, &vs[i], scenes[0].s.dx);
                     fvv[i] = filter_of(b.L, true, &vs[i], scenes[0].s.dx);
                     if (vs[i].persistent && !one_filter_pair(all[i], fpv[i], fvv[i])) all[i].clear();
+                    if (vs[i].smem_for(b.rc) > (size_t)smem_optin) all[i].clear();   // staging too large
                 }
                 upload_tables();
                 float best = 1e30f;
@@ -555,8 +566,13 @@ struct Kernel {
                     if (all[i].empty()) continue;
                     DevBuf<DevJob> tj;
                     tj.upload(all[i]);
-                    StageArgs a = stage_args(cur, 1, tj.p, dtw.p + twv[i], fpv[i], fvv[i]);
-                    for (int w = 0; w < 2; w++) CK(vs[i].launch((int)all[i].size(), a, stream));
+                    StageArgs a = stage_args(cur, 1, tj.p, dtw.p + twv[i], fpv[i], fvv[i], b.rc);
+                    if (vs[i].launch((int)all[i].size(), a, stream) != cudaSuccess) {
+                        cudaGetLastError();   // this variant's staging does not fit the bucket's strips
+                        rec += " " + std::to_string(i) + ":n/a";
+                        continue;
+                    }
+                    CK(vs[i].launch((int)all[i].size(), a, stream));
                     CK(cudaEventRecord(e0, stream));
                     const int reps = 5;
                     for (int w = 0; w < reps; w++) CK(vs[i].launch((int)all[i].size(), a, stream));
@@ -643,7 +659,7 @@ struct Kernel {
                     auto& b = buckets[i];
                     cudaStream_t s = i == 0 ? st : side[i];
                     if (i > 0) CK(cudaStreamWaitEvent(s, fork, 0));
-                    StageArgs a = stage_args(c, k, djobs.p + b.off, dtw.p + b.tw_off, b.fp_off, b.fv_off);
+                    StageArgs a = stage_args(c, k, djobs.p + b.off, dtw.p + b.tw_off, b.fp_off, b.fv_off, b.rc);
                     CK(b.var->launch(b.n, a, s));
                     if (i > 0) {
                         cudaEvent_t j = mk();
@@ -654,7 +670,7 @@ struct Kernel {
                 for (auto j : joins) CK(cudaStreamWaitEvent(st, j, 0));
             } else {
                 for (auto& b : buckets) {
-                    StageArgs a = stage_args(c, k, djobs.p + b.off, dtw.p + b.tw_off, b.fp_off, b.fv_off);
+                    StageArgs a = stage_args(c, k, djobs.p + b.off, dtw.p + b.tw_off, b.fp_off, b.fv_off, b.rc);
                     CK(b.var->launch(b.n, a, st));
                 }
             }
@@ -1354,6 +1370,7 @@ static int solve_noalloc(const pstd_config* config, int n_steps, float* frame_de
             a.att = F(o_att);
             a.stage = k;
             a.last = k == 5;
+            a.row_cap = 0;
             for (const NB& b : nbs) {
                 a.jobs = djobs + b.off;
                 a.tw = tw + b.tw;

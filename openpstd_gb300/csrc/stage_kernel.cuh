@@ -28,7 +28,12 @@
 //                    job j-1 while FFT warps transform job j (two shared-
 //                    memory buffers handed over with named barriers); the
 //                    twiddle tables and both derivative filters are staged in
-//                    shared memory once per CTA.
+//                    shared memory once per CTA;
+//   stage_pipe    -- persistent, all warps do every step; the strips, bands
+//                    and stage-start values of job k+2 are copied to shared
+//                    memory with cp.async while job k is transformed.
+// The autotuner times every form on the bucket's own jobs and keeps the
+// fastest (the pipelined form wins for the short PML-normal strips).
 //
 // Packing two real strips into one complex strip is exact in real
 // arithmetic: the filter is Hermitian, so the operator is real and acts on
@@ -295,13 +300,29 @@ __device__ __forceinline__ float band_value(float raw, float mirror, float T, fl
     return __fmul_rn(__fadd_rn(__fmul_rn(raw, T), __fmul_rn(mirror, R)), w);
 }
 
+// Field loads bypass L1 (the fields are streamed once per job), so that L1
+// keeps the twiddle, filter and window tables every CTA of a bucket reads.
+__device__ __forceinline__ float ldf(const float* p) {
+    float v;
+    asm("ld.global.nc.L1::no_allocate.f32 %0, [%1];" : "=f"(v) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ float4 ldf4(const float* p) {   // p 16-byte aligned
+    float4 v;
+    asm("ld.global.nc.L1::no_allocate.v4.f32 {%0, %1, %2, %3}, [%4];"
+        : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+        : "l"(p));
+    return v;
+}
+__device__ __forceinline__ void prefetch_l2(const float* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
 // Source of the strip data of one domain in one stage.
 struct Src {
     const float* a;   // p0 array (stale) or px, or the velocity field
     const float* b;   // py (p0 formed on the fly) or nullptr
     int pitch;
     __device__ __forceinline__ float at(long long e) const {
-        return b ? __fadd_rn(__ldg(a + e), __ldg(b + e)) : __ldg(a + e);
+        return b ? __fadd_rn(ldf(a + e), ldf(b + e)) : ldf(a + e);
     }
 };
 
@@ -327,11 +348,11 @@ __device__ __forceinline__ Src strip_source(const StageArgs& A, const DevDomain&
 __device__ __forceinline__ float4 ld4(const float* p, int i, int n) {
     float4 u = make_float4(0.f, 0.f, 0.f, 0.f);
     if (i + 4 <= n) {
-        u = __ldg(reinterpret_cast<const float4*>(p + i));
+        u = ldf4(p + i);
     } else {
-        u.x = __ldg(p + i);
-        if (i + 1 < n) u.y = __ldg(p + i + 1);
-        if (i + 2 < n) u.z = __ldg(p + i + 2);
+        u.x = ldf(p + i);
+        if (i + 1 < n) u.y = ldf(p + i + 1);
+        if (i + 2 < n) u.z = ldf(p + i + 2);
     }
     return u;
 }
@@ -421,6 +442,33 @@ __device__ __forceinline__ void gather(float2* sm, const StageArgs& A, const Dev
                 }
             }
         }
+    } else if (S2 % 4 == 0 && count == S2 && (job.first & 3) == 0) {
+        // columns, four adjacent strips per 16-byte load (rows are 128-byte
+        // aligned and the job starts on a multiple of four columns); four
+        // quads per thread in flight
+        constexpr int G = S2 / 4;
+        const int total = G * n;
+        for (int f0 = tid; f0 < total; f0 += 4 * NTH) {
+            float4 u[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int f = f0 + q * NTH;
+                if (f < total) {
+                    const int g = f % G, i = f / G;
+                    const float* a = S.a + (long long)i * S.pitch + job.first + 4 * g;
+                    u[q] = S.b ? add4(ldf4(a), ldf4(S.b + (a - S.a))) : ldf4(a);
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int f = f0 + q * NTH;
+                if (f < total) {
+                    const int g = f % G, i = f / G;
+                    sm[2 * g * SP + W + i] = make_float2(u[q].x, u[q].y);
+                    sm[(2 * g + 1) * SP + W + i] = make_float2(u[q].z, u[q].w);
+                }
+            }
+        }
     } else {
         // columns: consecutive threads read consecutive columns of one row,
         // four elements per thread in flight
@@ -503,6 +551,53 @@ __device__ __forceinline__ void gather(float2* sm, const StageArgs& A, const Dev
         for (int p = z0 + lane; p < L; p += 32) sm[cs * SP + p] = make_float2(0.f, 0.f);
 }
 
+// ---- L2 prefetch of everything a job streams: the strip rows / columns of
+// the gather and the stage-start values the epilogue reads (128-byte lines;
+// rows start on line boundaries, so every line touched lies inside its row)
+template <class C, int NTH>
+__device__ __forceinline__ void prefetch_job(const StageArgs& A, const DevJob& job, const DevDomain& dom, bool first,
+                                             int tid) {
+    const bool vel = job.kind & JK_VEL;
+    const bool ydir = job.kind & JK_Y;
+    const int n = (ydir ? dom.ny : dom.nx) + (vel ? 1 : 0);
+    const int nout = vel ? n - 1 : n + 1;
+    const Src S = strip_source(A, dom, vel, ydir, first);
+    long long fo;
+    int fp;
+    if (!vel) { fo = ydir ? dom.o_vy : dom.o_vx; fp = ydir ? dom.pitch_vy : dom.pitch_vx; }
+    else { fo = ydir ? dom.o_py : dom.o_px; fp = dom.pitch_p; }
+    const float* P = A.prev + fo;
+    const int count = job.count;
+    if (!ydir) {
+        const int li = (n + 31) >> 5, lo = (nout + 31) >> 5;
+        const int nin = S.b ? 2 * li : li, per_row = nin + lo;
+        for (int k = tid; k < count * per_row; k += NTH) {
+            const int s = k / per_row, l = k - s * per_row;
+            const long long row = job.first + s;
+            if (l < li) prefetch_l2(S.a + row * S.pitch + 32 * l);
+            else if (l < nin) prefetch_l2(S.b + row * S.pitch + 32 * (l - li));
+            else prefetch_l2(P + row * fp + 32 * (l - nin));
+        }
+    } else {
+        // the count-float segment of a row spans one line, or two
+        const int c0 = job.first, c1 = job.first + count - 1;
+        const bool two = (c0 >> 5) != (c1 >> 5);
+        for (int i = tid; i < n; i += NTH) {
+            const long long e = (long long)i * S.pitch;
+            prefetch_l2(S.a + e + c0);
+            if (two) prefetch_l2(S.a + e + c1);
+            if (S.b) {
+                prefetch_l2(S.b + e + c0);
+                if (two) prefetch_l2(S.b + e + c1);
+            }
+        }
+        for (int i = tid; i < nout; i += NTH) {
+            prefetch_l2(P + (long long)i * fp + c0);
+            if (two) prefetch_l2(P + (long long)i * fp + c1);
+        }
+    }
+}
+
 // ---- step 5: slice, RK update, (sixth stage) PML on vx / vy
 // RK update of one value in the reference's operation order
 // (kernel/Solver.cpp:174-181): v0 - (dt*a_k) * (L / rho) and p0 - (dt*a_k) * ((L*rho)*c^2)
@@ -583,6 +678,37 @@ __device__ __forceinline__ void epilogue(const float2* sm, const StageArgs& A, c
                 }
             }
         }
+    } else if (S2 % 4 == 0 && count == S2 && (job.first & 3) == 0) {
+        // columns, four adjacent strips per 16-byte load / store, four quads in flight
+        constexpr int G = S2 / 4;
+        const int total = G * nout;
+        for (int f0 = tid; f0 < total; f0 += 4 * NTH) {
+            float4 pv[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int f = f0 + q * NTH;
+                if (f < total) {
+                    const int g = f % G, i = f / G;
+                    pv[q] = ldf4(prev + fo + (long long)i * fp + job.first + 4 * g);
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int f = f0 + q * NTH;
+                if (f >= total) continue;
+                const int g = f % G, i = f / G;
+                const float2 d0 = sm[2 * g * SP + W + i], d1 = sm[(2 * g + 1) * SP + W + i];
+                float v[4] = {rk_update(pv[q].x, d0.x, vel, cdt, rho, c2), rk_update(pv[q].y, d0.y, vel, cdt, rho, c2),
+                              rk_update(pv[q].z, d1.x, vel, cdt, rho, c2), rk_update(pv[q].w, d1.y, vel, cdt, rho, c2)};
+                if (att) {
+                    const float a = A.att[ao + i];
+#pragma unroll
+                    for (int e = 0; e < 4; e++) v[e] = __fmul_rn(v[e], a);
+                }
+                *reinterpret_cast<float4*>(out + fo + (long long)i * fp + job.first + 4 * g) =
+                    make_float4(v[0], v[1], v[2], v[3]);
+            }
+        }
     } else {
         // columns: consecutive threads on consecutive columns, four values in flight
         const int total = S2 * nout;
@@ -592,7 +718,7 @@ __device__ __forceinline__ void epilogue(const float2* sm, const StageArgs& A, c
             for (int q = 0; q < 4; q++) {
                 const int f = f0 + q * NTH;
                 const int s = f % S2, i = f / S2;
-                pv[q] = (f < total && s < count) ? prev[fo + (long long)i * fp + job.first + s] : 0.f;
+                pv[q] = (f < total && s < count) ? ldf(prev + fo + (long long)i * fp + job.first + s) : 0.f;
             }
 #pragma unroll
             for (int q = 0; q < 4; q++) {
@@ -619,6 +745,7 @@ __global__ void __launch_bounds__(C::NT, C::MINB) stage_kernel(StageArgs A) {
         return;
     }
     const bool first = A.first_step[dom.scene] != 0;
+    prefetch_job<C, C::NT>(A, job, dom, first, threadIdx.x);
     gather<C, C::NT>(sm, A, job, dom, first, threadIdx.x);
     __syncthreads();
     convolve<C, C::NT, 0, false>(sm, A.tw, A.filt + job.dtab, threadIdx.x);
@@ -686,6 +813,351 @@ __global__ void __launch_bounds__(C::NT + C::NTP, 1) stage_ws(StageArgs A, int n
     }
 }
 
+// ---------------------------------------------------------------- pipelined form
+// Persistent CTAs walk the job list; the strips, interface bands and
+// stage-start values of job k+2 are copied global -> shared with cp.async
+// (no registers held, every copy of a job in flight at once) while job k is
+// transformed.  Each thread waits only for its own copy groups
+// (cp.async.wait_group) and a CTA barrier then publishes them, so there is no
+// spin wait.  Shared memory: the FFT buffer, then two staging slots of
+//   A[S2][rc] / B[S2][rc] / P[S2][rc]   (rows of x jobs; [rc][S2] for y jobs)
+//   bands[2 sides][2 fields][S2][32]
+// where A = px (or vx, vy, stale p0), B = py (p0 formed as A + B), P = the
+// stage-start values of the updated field.
+constexpr int PIPE_WB = 32;   // band slots per strip (windows are at most 32 wide)
+
+__device__ __forceinline__ void cp16(float* dst, const float* src) {   // both 16-byte aligned
+    const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp4(float* dst, const float* src) {
+    const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
+__host__ __device__ constexpr int pipe_slot_floats(int S2, int rc) { return 3 * S2 * rc + 4 * S2 * PIPE_WB; }
+
+// geometry of one job shared by staging, blending and the epilogue
+struct PipeJob {
+    bool vel, ydir, vec;   // vec: y job on four-aligned full columns (16-byte copies)
+    int n, nout, W, count;
+    long long fo;          // offset of the updated field in a state set
+    int fp, ao;            // its pitch; attenuation offset (-1 = none)
+    Src S;
+};
+
+template <int S2>
+__device__ __forceinline__ PipeJob pipe_job(const StageArgs& A, const DevJob& job, const DevDomain& dom, bool first) {
+    PipeJob g;
+    g.vel = job.kind & JK_VEL;
+    g.ydir = job.kind & JK_Y;
+    g.n = (g.ydir ? dom.ny : dom.nx) + (g.vel ? 1 : 0);
+    g.nout = g.vel ? g.n - 1 : g.n + 1;
+    g.W = job.W;
+    g.count = job.count;
+    g.vec = g.ydir && S2 % 4 == 0 && job.count == S2 && (job.first & 3) == 0;
+    if (!g.vel) {
+        g.fo = g.ydir ? dom.o_vy : dom.o_vx;
+        g.fp = g.ydir ? dom.pitch_vy : dom.pitch_vx;
+        g.ao = g.ydir ? dom.att_yv : dom.att_xv;
+    } else {
+        g.fo = g.ydir ? dom.o_py : dom.o_px;
+        g.fp = dom.pitch_p;
+        g.ao = -1;
+    }
+    g.S = strip_source(A, dom, g.vel, g.ydir, first);
+    return g;
+}
+
+// issue every copy of one job into `slot` (all NTH threads)
+template <class C, int NTH>
+__device__ __forceinline__ void pipe_stage_in(float* slot, const StageArgs& A, const DevJob& job, int rc, int tid) {
+    constexpr int S2 = 2 * C::CS;
+    const DevDomain dom = A.doms[job.dom];
+    const bool first = A.first_step[dom.scene] != 0;
+    const PipeJob g = pipe_job<S2>(A, job, dom, first);
+    float* sa = slot;
+    float* sb = slot + S2 * rc;
+    float* sp = slot + 2 * S2 * rc;
+    float* sband = slot + 3 * S2 * rc;
+    const float* P = A.prev + g.fo;
+    const Src& S = g.S;
+    const int nf = S.b ? 2 : 1;
+    if (!g.ydir) {
+        // rows: whole 16-byte quads (the last one reads into the row's padding)
+        const int qa = (g.n + 3) >> 2, qp = (g.nout + 3) >> 2;
+        const int per = nf * qa + qp;
+        for (int k = tid; k < g.count * per; k += NTH) {
+            const int s = k / per, q = k - s * per;
+            const long long row = job.first + s;
+            if (q < qa) cp16(sa + s * rc + 4 * q, S.a + row * S.pitch + 4 * q);
+            else if (q < nf * qa) cp16(sb + s * rc + 4 * (q - qa), S.b + row * S.pitch + 4 * (q - qa));
+            else cp16(sp + s * rc + 4 * (q - nf * qa), P + row * g.fp + 4 * (q - nf * qa));
+        }
+    } else if (g.vec) {
+        constexpr int G = S2 / 4;
+        const int tin = g.n * G;
+        for (int k = tid; k < nf * tin + g.nout * G; k += NTH) {
+            if (k < nf * tin) {
+                const int f = k >= tin, r = k - f * tin;
+                const int q = r % G, i = r / G;
+                cp16((f ? sb : sa) + i * S2 + 4 * q, (f ? S.b : S.a) + (long long)i * S.pitch + job.first + 4 * q);
+            } else {
+                const int r = k - nf * tin, q = r % G, i = r / G;
+                cp16(sp + i * S2 + 4 * q, P + (long long)i * g.fp + job.first + 4 * q);
+            }
+        }
+    } else {
+        // columns of a ragged or unaligned job: 4-byte copies
+        const int tin = g.n * g.count;
+        for (int k = tid; k < nf * tin + g.nout * g.count; k += NTH) {
+            if (k < nf * tin) {
+                const int f = k >= tin, r = k - f * tin;
+                const int s = r % g.count, i = r / g.count;
+                cp4((f ? sb : sa) + i * S2 + s, (f ? S.b : S.a) + (long long)i * S.pitch + job.first + s);
+            } else {
+                const int r = k - nf * tin, s = r % g.count, i = r / g.count;
+                cp4(sp + i * S2 + s, P + (long long)i * g.fp + job.first + s);
+            }
+        }
+    }
+    // interface bands of the neighbours: the W values next to the interface
+    const int W = g.W;
+    for (int d = 0; d < 2; d++) {
+        const int nb = d ? job.d2 : job.d1;
+        if (nb < 0) continue;
+        const DevDomain D = A.doms[nb];
+        const Src T = strip_source(A, D, g.vel, g.ydir, first);
+        const int nn = (g.ydir ? D.ny : D.nx) + (g.vel ? 1 : 0);
+        const int e0 = d ? (g.vel ? 1 : 0) : (g.vel ? nn - W - 1 : nn - W);
+        const int o = d ? job.o2 : job.o1;
+        // pressure bands keep two fields (px, py); a neighbour that supplies
+        // one (stale p0) gets a zero second field, so the blend adds exactly
+        const int tf = g.count * W;
+        for (int k = tid; k < (g.vel ? 1 : 2) * tf; k += NTH) {
+            const int f = k >= tf, r = k - f * tf;
+            const int s = r / W, j = r - s * W;
+            float* dst = sband + ((2 * d + f) * S2 + s) * PIPE_WB + j;
+            if (f && !T.b) {
+                *dst = 0.f;
+                continue;
+            }
+            const float* src = f ? T.b : T.a;
+            const long long e = g.ydir ? (long long)(e0 + j) * T.pitch + o + s : (long long)(o + s) * T.pitch + e0 + j;
+            cp4(dst, src + e);
+        }
+    }
+}
+
+// staged own strip value s at index i (p0 formed as A + B)
+template <int S2>
+__device__ __forceinline__ float pipe_own(const float* sa, const float* sb, bool two, bool ydir, int rc, int s, int i) {
+    const int e = ydir ? i * S2 + s : s * rc + i;
+    return two ? __fadd_rn(sa[e], sb[e]) : sa[e];
+}
+
+// staging slot -> complex strips of the FFT buffer (bands blended, zero padded)
+template <class C, int NTH>
+__device__ __forceinline__ void pipe_blend(float2* sm, const float* slot, const StageArgs& A, const DevJob& job,
+                                           const PipeJob& g, int rc, int tid) {
+    constexpr int CS = C::CS, SP = C::SP, L = C::L, S2 = 2 * CS;
+    const float* sa = slot;
+    const float* sb = slot + S2 * rc;
+    const float* sband = slot + 3 * S2 * rc;
+    const bool two = g.S.b != nullptr;
+    const int W = g.W, n = g.n;
+    const float* wl = A.win + job.wtab;          // window.head(W)
+    const float* wr = A.win + job.wtab + W + 1;  // window.tail(W)
+    for (int it = tid; it < CS * L; it += NTH) {
+        // x jobs: consecutive threads along a strip; y jobs: along the strip pairs
+        const int cs = g.ydir ? it % CS : it / L;
+        const int p = g.ydir ? it / CS : it % L;
+        float v[2];
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int s = 2 * cs + h;
+            float val = 0.f;
+            if (s < g.count) {
+                if (p < W) {
+                    if (job.d1 >= 0) {
+                        const float* b = sband + (0 * S2 + s) * PIPE_WB + p;
+                        const float raw = g.vel ? b[0] : __fadd_rn(b[0], b[S2 * PIPE_WB]);
+                        const int m = g.vel ? W - p : W - 1 - p;
+                        val = band_value(raw, pipe_own<S2>(sa, sb, two, g.ydir, rc, s, m), job.T1, job.R1, __ldg(wl + p));
+                    }
+                } else if (p < W + n) {
+                    val = pipe_own<S2>(sa, sb, two, g.ydir, rc, s, p - W);
+                } else if (p < 2 * W + n) {
+                    const int jj = p - W - n;
+                    if (job.d2 >= 0) {
+                        const float* b = sband + (2 * S2 + s) * PIPE_WB + jj;
+                        const float raw = g.vel ? b[0] : __fadd_rn(b[0], b[S2 * PIPE_WB]);
+                        const int m = g.vel ? n - 2 - jj : n - 1 - jj;
+                        val = band_value(raw, pipe_own<S2>(sa, sb, two, g.ydir, rc, s, m), job.T2, job.R2, __ldg(wr + jj));
+                    }
+                }
+            }
+            v[h] = val;
+        }
+        sm[cs * SP + p] = make_float2(v[0], v[1]);
+    }
+}
+
+// slice, RK update against the staged stage-start values, store
+template <class C, int NTH>
+__device__ __forceinline__ void pipe_epilogue(const float2* sm, const float* slot, const StageArgs& A, const DevJob& job,
+                                              const DevDomain& dom, const PipeJob& g, int rc, int tid) {
+    constexpr int CS = C::CS, SP = C::SP, S2 = 2 * CS;
+    const float* sp = slot + 2 * S2 * rc;
+    float* __restrict__ out = A.out;
+    const float cdt = A.doms[job.dom].cdt[A.stage];
+    const float rho = dom.rho, c2 = dom.c2;
+    const int W = g.W, nout = g.nout;
+    const bool att = A.last && g.ao >= 0;
+    if (!g.ydir) {
+        const int qn = (nout + 3) >> 2;
+        for (int k = tid; k < g.count * qn; k += NTH) {
+            const int s = k / qn, i = 4 * (k - s * qn);
+            const float4 pv = *reinterpret_cast<const float4*>(sp + s * rc + i);
+            const float* dv = reinterpret_cast<const float*>(sm + (s >> 1) * SP + W + i) + (s & 1);
+            float v[4] = {pv.x, pv.y, pv.z, pv.w};
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                v[e] = rk_update(v[e], dv[2 * e], g.vel, cdt, rho, c2);
+                if (att && i + e < nout) v[e] = __fmul_rn(v[e], A.att[g.ao + i + e]);
+            }
+            float* o = out + g.fo + (long long)(job.first + s) * g.fp + i;
+            if (i + 4 <= nout) {
+                *reinterpret_cast<float4*>(o) = make_float4(v[0], v[1], v[2], v[3]);
+            } else {
+#pragma unroll
+                for (int e = 0; e < 4; e++)
+                    if (i + e < nout) o[e] = v[e];
+            }
+        }
+    } else if (g.vec) {
+        constexpr int G = S2 / 4;
+        for (int k = tid; k < G * nout; k += NTH) {
+            const int q = k % G, i = k / G;
+            const float4 pv = *reinterpret_cast<const float4*>(sp + i * S2 + 4 * q);
+            const float2 d0 = sm[2 * q * SP + W + i], d1 = sm[(2 * q + 1) * SP + W + i];
+            float v[4] = {rk_update(pv.x, d0.x, g.vel, cdt, rho, c2), rk_update(pv.y, d0.y, g.vel, cdt, rho, c2),
+                          rk_update(pv.z, d1.x, g.vel, cdt, rho, c2), rk_update(pv.w, d1.y, g.vel, cdt, rho, c2)};
+            if (att) {
+                const float a = A.att[g.ao + i];
+#pragma unroll
+                for (int e = 0; e < 4; e++) v[e] = __fmul_rn(v[e], a);
+            }
+            *reinterpret_cast<float4*>(out + g.fo + (long long)i * g.fp + job.first + 4 * q) =
+                make_float4(v[0], v[1], v[2], v[3]);
+        }
+    } else {
+        const float* smf = reinterpret_cast<const float*>(sm);
+        for (int k = tid; k < g.count * nout; k += NTH) {
+            const int s = k % g.count, i = k / g.count;
+            float v = rk_update(sp[i * S2 + s], smf[2 * ((s >> 1) * SP + W + i) + (s & 1)], g.vel, cdt, rho, c2);
+            if (att) v = __fmul_rn(v, A.att[g.ao + i]);
+            out[g.fo + (long long)i * g.fp + job.first + s] = v;
+        }
+    }
+}
+
+template <class C>
+__global__ void __launch_bounds__(C::NT, C::MINB) stage_pipe(StageArgs A, int n_jobs) {
+    constexpr int NT = C::NT, S2 = 2 * C::CS;
+    extern __shared__ float2 sm[];
+    const int rc = A.row_cap;
+    float* slots = reinterpret_cast<float*>(sm + C::BUF);
+    const int slot_f = pipe_slot_floats(S2, rc);
+    const int tid = threadIdx.x;
+    const int stride = gridDim.x;
+    const int mine = (int)blockIdx.x < n_jobs ? (n_jobs - 1 - (int)blockIdx.x) / stride + 1 : 0;
+    // prologue: jobs 0 and 1 of this CTA in flight
+    for (int k = 0; k < 2; k++) {
+        if (k < mine) {
+            const DevJob job = A.jobs[blockIdx.x + k * stride];
+            if (!(job.kind & JK_COPY)) pipe_stage_in<C, NT>(slots + k * slot_f, A, job, rc, tid);
+        }
+        cp_commit();
+    }
+    for (int k = 0; k < mine; k++) {
+        const float* slot = slots + (k & 1) * slot_f;
+        cp_wait1();
+        __syncthreads();
+        const DevJob job = A.jobs[blockIdx.x + k * stride];
+        const DevDomain dom = A.doms[job.dom];
+        if (job.kind & JK_COPY) {
+            copy_axis<NT>(A, dom, job.kind & JK_Y, tid);
+        } else {
+            const PipeJob g = pipe_job<S2>(A, job, dom, A.first_step[dom.scene] != 0);
+            pipe_blend<C, NT>(sm, slot, A, job, g, rc, tid);
+            __syncthreads();
+            convolve<C, NT, 0, false>(sm, A.tw, A.filt + job.dtab, tid);
+            __syncthreads();
+            pipe_epilogue<C, NT>(sm, slot, A, job, dom, g, rc, tid);
+        }
+        __syncthreads();   // the slot and the FFT buffer are free again
+        if (k + 2 < mine) {
+            const DevJob nxt = A.jobs[blockIdx.x + (k + 2) * stride];
+            if (!(nxt.kind & JK_COPY)) pipe_stage_in<C, NT>(slots + (k & 1) * slot_f, A, nxt, rc, tid);
+        }
+        cp_commit();
+    }
+}
+
+template <class C>
+size_t pipe_smem(int rc) {
+    return (size_t)C::BUF * 8 + 2 * (size_t)pipe_slot_floats(2 * C::CS, rc) * 4;
+}
+
+template <class C>
+cudaError_t launch_pipe_t(int n_jobs, const StageArgs& a, cudaStream_t st) {
+    static int sms = 0, optin = 0;
+    if (sms == 0) {
+        int dev;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    }
+    const size_t smem = pipe_smem<C>(a.row_cap);
+    if (a.row_cap < 4 || (a.row_cap & 3) || smem > (size_t)optin) return cudaErrorInvalidValue;   // does not fit
+    int per = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, stage_pipe<C>, C::NT, smem);
+    const int grid_max = sms * (per > 0 ? per : 1);
+    const int g = n_jobs < grid_max ? n_jobs : grid_max;
+    stage_pipe<C><<<g, C::NT, smem, st>>>(a, n_jobs);
+    return cudaGetLastError();
+}
+
+template <class C>
+cudaError_t prepare_pipe_t() {
+    int dev, optin;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    return cudaFuncSetAttribute(stage_pipe<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+}
+
+template <class C>
+size_t plain_smem(int) {
+    return (size_t)C::SMEM;
+}
+
+template <class C>
+StageVariant make_pipe_variant(const char* name) {
+    StageVariant v;
+    v.L = C::L; v.CS = C::CS; v.NT = C::NT; v.smem = 0; v.np = C::NP;
+    v.r[0] = C::R0; v.r[1] = C::R1; v.r[2] = C::R2; v.r[3] = C::R3;
+    v.persistent = false;
+    v.pipe = true;
+    v.launch = &launch_pipe_t<C>;
+    v.prepare = &prepare_pipe_t<C>;
+    v.smem_for = &pipe_smem<C>;
+    v.name = name;
+    return v;
+}
+
 template <class C>
 cudaError_t launch_stage_t(int n_jobs, const StageArgs& a, cudaStream_t st) {
     if constexpr (C::NTP > 0) {
@@ -719,8 +1191,10 @@ StageVariant make_variant(const char* name) {
     v.L = C::L; v.CS = C::CS; v.NT = C::NT + C::NTP; v.smem = C::SMEM; v.np = C::NP;
     v.r[0] = C::R0; v.r[1] = C::R1; v.r[2] = C::R2; v.r[3] = C::R3;
     v.persistent = C::NTP > 0;
+    v.pipe = false;
     v.launch = &launch_stage_t<C>;
     v.prepare = &prepare_stage_t<C>;
+    v.smem_for = &plain_smem<C>;
     v.name = name;
     return v;
 }

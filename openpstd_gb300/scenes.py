@@ -117,6 +117,18 @@ def plain_square(seed: int = 0, n: int = 200, steps: int = 500, pml: int = 50, n
     return conf
 
 
+def rect(seed: int = 0, nx: int = 1200, ny: int = 100, steps: int = 50, pml: int = 50, n_receivers: int = 2,
+         dx: float = 0.2) -> PSTDConfiguration:
+    """Single nx x ny domain with absorbing PML on all four edges (long x strips)."""
+    rng = np.random.default_rng(seed)
+    conf = PSTDConfiguration()
+    base_settings(conf, steps, dx=dx, pml=pml)
+    conf.Domains = [_domain(0, 0, nx, ny, dx, dict(left=1.0, right=1.0, top=1.0, bottom=1.0))]
+    conf.Speakers = [_point_in(rng, 0, 0, nx, ny, dx)]
+    conf.Receivers = [_receiver_in(rng, (0, 0, nx, ny), dx) for _ in range(n_receivers)]
+    return conf
+
+
 def l_shape(seed: int = 0, scale: float = 1.0, steps: int = 4000, pml: int = 50, n_speakers: int = 4,
             n_receivers: int = 16, dx: float = 0.2) -> PSTDConfiguration:
     """A (2a x a) + B (a x a) + C (a x 2a), a = 600*scale cells, as an L."""

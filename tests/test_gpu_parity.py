@@ -238,14 +238,18 @@ def test_full_size_l_shape_superposition():
         assert rel(b, a) < 1e-5, f
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5, 6])
 def test_every_stage_variant(oracle_mod, variant, monkeypatch):
     """Each compiled stage-kernel variant (strips per CTA, threads, radix
     plan) must reproduce the oracle: the autotuner may pick any of them."""
     from openpstd_gb300 import scenes
     monkeypatch.setenv("PSTD_VARIANT", str(variant))
-    conf = scenes.l_shape(2, scale=0.5, steps=60)      # transform lengths 128, 1024, 2048
+    conf = scenes.l_shape(2, scale=0.5, steps=60)      # transform lengths 128, 512, 1024
     _, rep = check_parity(oracle_mod, conf, 60, threads=16)
     print(variant, rep)
-    conf = scenes.plain_square(1, n=180, steps=40)     # 128, 256 (and 512 for the 180-cell strips)
+    conf = scenes.plain_square(1, n=180, steps=40)     # 128, 256
     check_parity(oracle_mod, conf, 40, threads=16)
+    conf = scenes.rect(4, nx=1200, ny=90, steps=30)    # 2048 (x strips), 256, 128
+    check_parity(oracle_mod, conf, 30, threads=16)
+    conf = scenes.rect(5, nx=2000, ny=60, steps=20)    # 4096 (x strips), 128
+    check_parity(oracle_mod, conf, 20, threads=16)
