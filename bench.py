@@ -1,6 +1,6 @@
 """Throughput of the GB300 PSTD solve (Gcell-steps/s).
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload lshape|square]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload lshape|square|batch|serve]
 
 Workload (default ``lshape``): the multi-domain L-shaped scene -- 1200x600,
 600x600 and 600x1200 air cells (dx = 0.2 m) with a seeded mix of rigid and
@@ -209,6 +209,85 @@ def run_batch(args):
     print(json.dumps(line), flush=True)
 
 
+def run_serve(args):
+    """Serving workload: Poisson arrivals (mean --rate per second) of
+    batch-like scenes with step counts log-uniform 200..8000, served by the
+    continuous-batching loop under an HBM budget for --duration seconds of
+    wall clock; latency = completion - arrival.  Beside it, the plain path
+    solving a sample of the same requests one at a time (create + steps)."""
+    import torch
+    from openpstd_gb300 import build as _b, scenes
+    from openpstd_gb300 import kernel
+    from openpstd_gb300.serving import Server
+    _b.build()
+    torch.cuda.set_device(0)
+    reqs = scenes.serving_requests(0, rate_hz=args.rate, duration_s=args.duration)
+    budget = int(args.budget_gb * (1 << 30))
+    srv = Server(budget, max_scenes=4096)
+    pending, live = 0, {}
+    lat, occ = [], []
+    t0 = time.perf_counter()
+    with ClockSampler(0) as clk:
+        while True:
+            now = time.perf_counter() - t0
+            if now >= args.duration:
+                break
+            while pending < len(reqs) and reqs[pending][0] <= now:
+                at, conf = reqs[pending]
+                rid = srv.submit(conf, conf.Settings.framecount())
+                live[rid] = at
+                pending += 1
+            info = srv.tick(args.tick_steps)
+            occ.append(srv.stats()["bytes_in_use"])
+            if info["finished"]:
+                t_done = time.perf_counter() - t0
+                for rid in list(live):
+                    if srv.poll(rid)["state"] == 2:
+                        lat.append(t_done - live.pop(rid))
+                        srv.result(rid)
+            if info["active"] == 0 and info["queued"] == 0 and pending < len(reqs):
+                time.sleep(max(0.0, min(reqs[pending][0] - (time.perf_counter() - t0), 0.01)))
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    served = st["cell_steps"] / wall / 1e9
+    # plain path, one request at a time (create + all its steps), on a sample
+    t_plain, cs_plain, n_plain = 0.0, 0, 0
+    for at, conf in reqs[: args.plain_requests]:
+        t1 = time.perf_counter()
+        k = kernel.PSTDKernel()
+        k.initialize_kernel(conf)
+        n = conf.Settings.framecount()
+        k.advance(n)
+        k.synchronize()
+        t_plain += time.perf_counter() - t1
+        cs_plain += k.work_counts()["cells"] * n
+        n_plain += 1
+        k.close()
+        if t_plain > args.plain_seconds:
+            break
+    plain = cs_plain / t_plain / 1e9
+    lat_s = sorted(lat)
+    pct = (lambda q: lat_s[min(len(lat_s) - 1, int(q * len(lat_s)))] if lat_s else None)
+    line = {"metric": METRIC, "value": served, "unit": METRIC, "n_gpus": 1, "steps": None, "warmup": 0,
+            "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded Poisson request stream)",
+            "config": {"workload": f"serving: Poisson {args.rate}/s of batch-like scenes (64x64..1024x768 cells, "
+                                   "1-6 rectangles), steps log-uniform 200..8000, HBM budget "
+                                   f"{args.budget_gb} GB, {args.duration} s wall clock",
+                       "tick_steps": args.tick_steps},
+            "latency_s": {"p50": pct(0.5), "p99": pct(0.99), "completed": len(lat)},
+            "requests": {"arrived": pending, "completed": st["done"], "active_at_end": st["active"],
+                         "queued_at_end": st["queued"]},
+            "hbm": {"budget_bytes": budget, "peak_bytes_in_use": st["peak_bytes"],
+                    "mean_occupancy": (sum(occ) / len(occ) / budget) if occ else 0.0},
+            "plan_rebuilds": st["rebuilds"],
+            "plain_serial": {"value": plain, "unit": METRIC, "requests": n_plain,
+                             "note": "the first requests solved one at a time with the plain path (create + steps)"},
+            "served_over_plain": served / plain if plain else None, "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args):
     rank, ws, dist = dist_setup()
     if rank != 0:
@@ -372,6 +451,12 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch-scenes", type=int, default=256)
     ap.add_argument("--plain-steps", type=int, default=50)
+    ap.add_argument("--rate", type=float, default=50.0, help="serve: mean request arrivals per second")
+    ap.add_argument("--duration", type=float, default=60.0, help="serve: seconds of wall clock")
+    ap.add_argument("--budget-gb", type=float, default=80.0, help="serve: HBM budget")
+    ap.add_argument("--tick-steps", type=int, default=64, help="serve: most steps per tick")
+    ap.add_argument("--plain-requests", type=int, default=40)
+    ap.add_argument("--plain-seconds", type=float, default=20.0)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -379,6 +464,8 @@ def main():
         run_reference(args)
     elif args.workload == "batch":
         run_batch(args)
+    elif args.workload == "serve":
+        run_serve(args)
     else:
         run_ours(args)
 

@@ -220,6 +220,42 @@ int pstd_plan_info(pstd_kernel* k, char* buf, int32_t cap);
  * per time step. */
 int pstd_work_counts(pstd_kernel* k, int64_t* cells, int64_t* air_cells, int32_t* launches_per_step);
 
+/* ---- serving loop (no counterpart in the reference) ----------------------
+ * Continuous batching of scene solves on one GPU.  The server reserves
+ * hbm_budget_bytes of device memory once (three state-set arenas, p0, rigid
+ * fields, receiver rings) and keeps at most max_scenes scenes active.
+ * pstd_server_submit builds the scene on the host and queues it; every
+ * pstd_server_tick admits queued requests in arrival order while their
+ * fields fit (admission by HBM footprint), advances all active scenes
+ * together -- one stage-kernel launch per strip length and RK stage over the
+ * strips of all of them, captured as CUDA graphs per membership -- by
+ * min(max_steps, steps left of the scene closest to completion), and hands
+ * finished scenes' receiver series (and, with PSTD_REQ_FINAL_FRAME, their
+ * last p0 frame) to the host.  Results equal a solo pstd_create +
+ * pstd_advance of the same scene with the same kernel variants.  One thread
+ * drives a server; calls are not re-entrant. */
+typedef struct pstd_server pstd_server;
+#define PSTD_REQ_QUEUED    0
+#define PSTD_REQ_ACTIVE    1
+#define PSTD_REQ_DONE      2
+#define PSTD_REQ_CANCELLED 3
+#define PSTD_REQ_FINAL_FRAME 1   /* submit flag: keep p0 of the non-PML domains after the last step */
+int pstd_server_create(int64_t hbm_budget_bytes, int32_t max_scenes, const pstd_callbacks* log_cb, pstd_server** out);
+void pstd_server_destroy(pstd_server* s);
+/* PSTD_ERR_NO_MEMORY if the scene alone exceeds the arenas */
+int pstd_server_submit(pstd_server* s, const pstd_config* config, int32_t n_steps, int32_t flags, int64_t* request_id);
+/* info (may be NULL): {active, queued, finished in this tick, steps advanced} */
+int pstd_server_tick(pstd_server* s, int32_t max_steps, int32_t* info);
+/* sizes (may be NULL): {receiver floats = n_steps x n_receivers, frame floats} */
+int pstd_server_poll(pstd_server* s, int64_t request_id, int32_t* state, int32_t* steps_done, int64_t* sizes);
+/* copy a finished request's results (sizes as pstd_server_poll reports) and forget it */
+int pstd_server_result(pstd_server* s, int64_t request_id, float* receivers, int64_t n_receivers, float* frame,
+                       int64_t n_frame);
+int pstd_server_cancel(pstd_server* s, int64_t request_id);
+/* stats[8] = {budget bytes, bytes in use, peak bytes in use, cell-steps done,
+ *             requests done, plan rebuilds, active, queued} */
+int pstd_server_stats(pstd_server* s, int64_t* stats);
+
 /* ---- allocation-free solve (no counterpart in the reference) ------------
  * For callers that cannot allocate device memory: host applications that
  * own the GPU's memory through their own pool or arena (a serving process

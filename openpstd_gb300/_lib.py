@@ -64,6 +64,14 @@ SIGNATURES = {
     "pstd_profile_passes": (ctypes.c_int, [_vp, _i32, _vp, _P(_f32), _P(_f32), _P(_i32), _P(_i32)]),
     "pstd_plan_info": (ctypes.c_int, [_vp, ctypes.c_char_p, _i32]),
     "pstd_work_counts": (ctypes.c_int, [_vp, _P(_i64), _P(_i64), _P(_i32)]),
+    "pstd_server_create": (ctypes.c_int, [_i64, _i32, _P(c_callbacks), _P(_vp)]),
+    "pstd_server_destroy": (None, [_vp]),
+    "pstd_server_submit": (ctypes.c_int, [_vp, _P(c_config), _i32, _i32, _P(_i64)]),
+    "pstd_server_tick": (ctypes.c_int, [_vp, _i32, _P(_i32)]),
+    "pstd_server_poll": (ctypes.c_int, [_vp, _i64, _P(_i32), _P(_i32), _P(_i64)]),
+    "pstd_server_result": (ctypes.c_int, [_vp, _i64, _P(_f32), _i64, _P(_f32), _i64]),
+    "pstd_server_cancel": (ctypes.c_int, [_vp, _i64]),
+    "pstd_server_stats": (ctypes.c_int, [_vp, _P(_i64)]),
     "pstd_solve_noalloc": (ctypes.c_int, [_P(c_config), _i32, _vp, _i64, _vp, _i64, _vp]),
     "pstd_last_error": (ctypes.c_char_p, []),
     "pstd_version": (ctypes.c_char_p, []),

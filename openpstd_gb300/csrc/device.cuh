@@ -65,4 +65,12 @@ struct DevSpeaker {
     float x, y;
 };
 
+// Receiver of a scene in the serving loop: its samples go to the scene's own
+// ring (step-major, `stride` receivers per step) at the scene's own step count.
+struct DevSrvReceiver {
+    int dom, row, col, slot;
+    long long ring;   // float offset of the scene's ring in the auxiliary arena
+    int stride, index;
+};
+
 }  // namespace pstd

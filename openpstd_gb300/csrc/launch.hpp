@@ -48,6 +48,10 @@ cudaError_t launch_speakers(const DevDomain* doms, const int* x0, const int* y0,
                             int n_spk, float dx, float bw, float* set, float* fixed, float* p0, cudaStream_t st);
 cudaError_t launch_receivers(const DevReceiver* rec, int n_rec, const DevDomain* doms, const float* set, float* ring,
                              int cap, int* counter, cudaStream_t st);
+// serving loop: one sample per receiver into its scene's ring at the scene's
+// step count, then every listed slot's step count + 1
+cudaError_t launch_server_receivers(const DevSrvReceiver* rec, int n_rec, const DevDomain* doms, const float* set,
+                                    float* aux, int* scene_step, const int* slots, int n_slots, cudaStream_t st);
 // dense p0 = px + py of the given domains into dst (frames)
 cudaError_t launch_frame(const int* doms_idx, const long long* dst_off, int n, const DevDomain* doms, const float* set,
                          float* dst, cudaStream_t st);

@@ -103,6 +103,20 @@ __global__ void receiver_kernel(const DevReceiver* rec, int n_rec, const DevDoma
     if (threadIdx.x == 0) *counter = step + 1;
 }
 
+__global__ void server_receiver_kernel(const DevSrvReceiver* rec, int n_rec, const DevDomain* doms,
+                                       const float* __restrict__ set, float* aux, int* scene_step, const int* slots,
+                                       int n_slots) {
+    for (int r = threadIdx.x; r < n_rec; r += blockDim.x) {
+        const DevSrvReceiver q = rec[r];
+        const DevDomain d = doms[q.dom];
+        const long long e = (long long)q.row * d.pitch_p + q.col;
+        const long long step = scene_step[q.slot];
+        aux[q.ring + step * q.stride + q.index] = __fadd_rn(set[d.o_px + e], set[d.o_py + e]);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < n_slots; i += blockDim.x) scene_step[slots[i]] += 1;
+}
+
 __global__ void frame_kernel(const int* idx, const long long* dst_off, const DevDomain* doms,
                              const float* __restrict__ set, float* dst) {
     const DevDomain d = doms[idx[blockIdx.y]];
@@ -132,6 +146,13 @@ cudaError_t launch_speakers(const DevDomain* doms, const int* x0, const int* y0,
 cudaError_t launch_receivers(const DevReceiver* rec, int n_rec, const DevDomain* doms, const float* set, float* ring,
                              int cap, int* counter, cudaStream_t st) {
     receiver_kernel<<<1, 256, 0, st>>>(rec, n_rec, doms, set, ring, cap, counter);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_server_receivers(const DevSrvReceiver* rec, int n_rec, const DevDomain* doms, const float* set,
+                                    float* aux, int* scene_step, const int* slots, int n_slots, cudaStream_t st) {
+    if (n_slots <= 0) return cudaSuccess;
+    server_receiver_kernel<<<1, 256, 0, st>>>(rec, n_rec, doms, set, aux, scene_step, slots, n_slots);
     return cudaGetLastError();
 }
 

@@ -28,6 +28,7 @@
 #include <vector>
 
 #include "../../include/pstd_gb300.h"
+#include "kernel_state.hpp"
 #include "launch.hpp"
 #include "scene.hpp"
 
@@ -35,686 +36,11 @@ namespace pstd {
 
 static thread_local std::string g_error;
 
-struct CudaError : std::runtime_error {
-    explicit CudaError(const std::string& m) : std::runtime_error(m) {}
-};
-
-#define CK(call)                                                                                          \
-    do {                                                                                                  \
-        cudaError_t e_ = (call);                                                                          \
-        if (e_ != cudaSuccess)                                                                            \
-            throw CudaError(std::string(#call) + ": " + cudaGetErrorString(e_));                          \
-    } while (0)
-
-template <class T>
-struct DevBuf {
-    T* p = nullptr;
-    size_t n = 0;
-    void alloc(size_t count) {
-        release();
-        n = count;
-        if (count) CK(cudaMalloc(&p, count * sizeof(T)));
-    }
-    void upload(const std::vector<T>& v) {
-        alloc(std::max<size_t>(v.size(), 1));
-        if (!v.empty()) CK(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
-    }
-    void release() {
-        if (p) cudaFree(p);
-        p = nullptr;
-        n = 0;
-    }
-    ~DevBuf() { release(); }
-};
-
-struct PinnedBuf {
-    float* p = nullptr;
-    size_t n = 0;
-    void alloc(size_t count) {
-        if (count <= n) return;
-        if (p) cudaFreeHost(p);
-        p = nullptr;
-        n = 0;
-        CK(cudaMallocHost(&p, count * sizeof(float)));
-        n = count;
-    }
-    ~PinnedBuf() { if (p) cudaFreeHost(p); }
-};
-
-// Position of spectrum bin k after the in-place decimation-in-frequency
-// transform with radices r[0..np): k = k1 + r1 k2 + r1 r2 k3 + ... sits at
-// k1 (L/r1) + k2 (L/(r1 r2)) + ...
-static std::vector<int> bin_positions(int L, const int* r, int np) {
-    std::vector<int> pos(L);
-    for (int k = 0; k < L; k++) {
-        int rem = k, span = L, p = 0;
-        for (int i = 0; i < np; i++) {
-            int d = rem % r[i];
-            rem /= r[i];
-            span /= r[i];
-            p += d * span;
-        }
-        pos[k] = p;
-    }
-    return pos;
+int set_error(int code, const std::string& message) {
+    g_error = message;
+    return code;
 }
 
-struct Bucket {
-    int L = 0;
-    const StageVariant* var = nullptr;
-    int off = 0, n = 0;            // jobs in djobs
-    int tw_off = 0;                // float2 offset of the twiddles in dtw
-    int fp_off = 0, fv_off = 0;    // float2 offsets of the pressure / velocity filters
-    int rc = 4;                    // floats staged per strip by the pipelined form
-    std::string choice;            // autotune record
-};
-
-struct Kernel {
-    std::vector<Scene> scenes;          // one per batch member (a single scene: one)
-    std::vector<int> dom_base;          // global index of each scene's first domain
-    std::vector<int> rec_base;          // global index of each scene's first receiver
-    std::vector<std::pair<int, int>> gdom;   // global domain -> (scene, local index)
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    std::vector<cudaStream_t> side;     // one per bucket, for concurrent capture
-    pstd_callbacks logcb{};
-    bool have_logcb = false;
-    bool host_only = false;             // built by pstd_scene_build: no device state
-    bool autotune = true;
-    int smem_optin = 0;                 // largest dynamic shared memory a CTA may opt in to
-
-    // layout
-    std::vector<DevDomain> hdoms;
-    size_t set_floats = 0, fixed_floats = 0, p0_floats = 0;
-    DevBuf<float> sets[3], init_set, fixed, init_fixed, p0, init_p0;
-    DevBuf<int> first_step;
-    int cur = 0;              // set holding the current (stage-start) state
-    int steps = 0;            // steps taken since reset
-    int framecount = 0;
-
-    DevBuf<DevDomain> ddoms;
-    DevBuf<DevJob> djobs;
-    DevBuf<float2> dfilt, dtw;
-    DevBuf<float> dwin, datt;
-    DevBuf<int> dpml;                 // indices of PML domains
-    int n_pml = 0;
-    DevBuf<DevReceiver> drec;
-    DevBuf<float> dring;
-    DevBuf<int> dcounter;
-    std::vector<Bucket> buckets;
-    int ring_cap = 1;
-    int n_rec = 0;
-    int64_t cells = 0, air_cells = 0;
-
-    // host-side tables
-    std::vector<float> win;
-    std::map<std::pair<int, int>, int> win_off;   // (W, patch error)
-    std::vector<float2> filt;
-    std::map<std::tuple<int, int, int, int, int, int, float>, int> filt_off;   // (L, vel, radices, dx)
-    std::vector<float2> tw;
-    std::map<std::tuple<int, int, int, int, int>, int> tw_off;   // (L, radices)
-
-    // frames
-    std::vector<int> frame_doms;
-    std::vector<long long> frame_off;
-    size_t frame_floats = 0;
-    DevBuf<int> dframe_doms;
-    DevBuf<long long> dframe_off;
-    DevBuf<float> dframe;
-
-    cudaGraphExec_t graphs[3] = {nullptr, nullptr, nullptr};
-    bool graphs_ok = false;
-
-    void log(int level, const std::string& m) {
-        if (have_logcb && logcb.log) logcb.log(logcb.user, level, m.c_str());
-    }
-
-    ~Kernel() {
-        for (auto& g : graphs) if (g) cudaGraphExecDestroy(g);
-        for (auto s : side) cudaStreamDestroy(s);
-        if (stream) cudaStreamDestroy(stream);
-    }
-
-    // ---------------------------------------------------------------- tables
-    const Domain& dom(int g) const { return scenes[gdom[g].first].doms[gdom[g].second]; }
-    const Scene& scene_of(int g) const { return scenes[gdom[g].first]; }
-
-    int window_of(int W, int patch) {
-        auto key = std::make_pair(W, patch);
-        auto it = win_off.find(key);
-        if (it != win_off.end()) return it->second;
-        int o = (int)win.size();
-        // kernel/core/kernel_functions.cpp:327-333 (patch error cast to int)
-        double walpha = (patch - 40) / 20.0 + 1;
-        for (int i = -W; i <= W; i++) {
-            double x = (double)i / W;
-            double x6 = x * x * x * x * x * x;
-            win.push_back((float)std::exp(-std::log(10.0) * walpha * x6));
-        }
-        win_off[key] = o;
-        return o;
-    }
-
-    int filter_of(int L, bool vel, const StageVariant* v, float dxf) {
-        auto key = std::make_tuple(L, (int)vel, v->r[0], v->r[1], v->r[2], v->r[3], dxf);
-        auto it = filt_off.find(key);
-        if (it != filt_off.end()) return it->second;
-        int o = (int)filt.size();
-        // kernel/core/WisdomCache.cpp:53-75: k_j = j (pi/dx)/(L/2) for bins
-        // 0..L/2, factor exp(-/+ i k dx/2) * i k; Hermitian extension; 1/L
-        const double dx = (double)dxf;
-        const double kmax = M_PI / dx;
-        std::vector<std::complex<double>> full(L);
-        for (int j = 0; j <= L / 2; j++) {
-            double k = kmax * j / (L / 2);
-            full[j] = std::exp(std::complex<double>(0, (vel ? 0.5 : -0.5) * k * dx)) * std::complex<double>(0, k);
-        }
-        full[0] = std::complex<double>(full[0].real(), 0);
-        full[L / 2] = std::complex<double>(full[L / 2].real(), 0);   // c2r ignores the Nyquist imaginary part
-        for (int j = 1; j < L / 2; j++) full[L - j] = std::conj(full[j]);
-        std::vector<int> pos = bin_positions(L, v->r, v->np);
-        std::vector<float2> perm(L);
-        for (int j = 0; j < L; j++) {
-            std::complex<double> c = full[j] / (double)L;
-            perm[pos[j]] = make_float2((float)c.real(), (float)c.imag());
-        }
-        filt.insert(filt.end(), perm.begin(), perm.end());
-        filt_off[key] = o;
-        return o;
-    }
-
-    // per-pass twiddle tables of a radix plan: pass p (block size M, radix R)
-    // holds [n1][k] = exp(-2 pi i n1 k / M) for n1 < M/R, k < R; the offset
-    // of every pass is a multiple of 2 float2 (16-byte loads)
-    int twiddles_of(const StageVariant* v) {
-        auto key = std::make_tuple(v->L, v->r[0], v->r[1], v->r[2], v->r[3]);
-        auto it = tw_off.find(key);
-        if (it != tw_off.end()) return it->second;
-        if (tw.size() & 1) tw.push_back(make_float2(0, 0));
-        int o = (int)tw.size();
-        int M = v->L;
-        for (int p = 0; p + 1 < v->np; p++) {
-            const int R = v->r[p], Q = M / R;
-            for (int n1 = 0; n1 < Q; n1++)
-                for (int k = 0; k < R; k++) {
-                    double a = -2.0 * M_PI * (double)n1 * k / M;
-                    tw.push_back(make_float2((float)std::cos(a), (float)std::sin(a)));
-                }
-            M = Q;
-        }
-        tw_off[key] = o;
-        return o;
-    }
-
-    static int run_length(const Scene& sc, const StripRun& r) {
-        int n = sc.doms[r.dom].len(r.axis);
-        return Scene::next_pow2(n + 2 * sc.window_for(n));
-    }
-
-    // all jobs of bucket L for variant v (+ copy jobs if `with_copies`);
-    // domain indices are global (scene base + local)
-    std::vector<DevJob> make_jobs(int L, const StageVariant* v, bool with_copies) {
-        std::vector<DevJob> jobs;
-        const int per = 2 * v->CS;
-        for (size_t si = 0; si < scenes.size(); si++) {
-            const Scene& sc = scenes[si];
-            const int base = dom_base[si];
-            for (const StripRun& r : sc.runs) {
-                if (run_length(sc, r) != L) continue;
-                const Domain& d = sc.doms[r.dom];
-                int n = d.len(r.axis);
-                int W = sc.window_for(n);
-                int wo = window_of(W, (int)sc.s.patcherror);
-                for (int vel = 0; vel < 2; vel++) {
-                    // reflection / transmission of the bands (kernel/core/kernel_functions.cpp:37-64)
-                    float rs = d.rho;
-                    float r1 = r.d1 >= 0 ? sc.doms[r.d1].rho : rs;
-                    float r2 = r.d2 >= 0 ? sc.doms[r.d2].rho : rs;
-                    float zn1 = r1 / rs, izn1 = rs / r1, zn2 = r2 / rs, izn2 = rs / r2;
-                    float rlw1 = (zn1 - 1) / (zn1 + 1), tlw1 = (2 * zn1) / (zn1 + 1), tlw2 = (2 * izn1) / (izn1 + 1);
-                    float rrw1 = (zn2 - 1) / (zn2 + 1), trw1 = (2 * zn2) / (zn2 + 1), trw2 = (2 * izn2) / (izn2 + 1);
-                    DevJob j;
-                    std::memset(&j, 0, sizeof j);
-                    j.dom = base + r.dom;
-                    j.kind = (vel ? JK_VEL : 0) | (r.axis == AX_Y ? JK_Y : 0);
-                    j.W = W;
-                    j.d1 = r.d1 >= 0 ? base + r.d1 : -1;
-                    j.d2 = r.d2 >= 0 ? base + r.d2 : -1;
-                    if (vel) { j.R1 = -rlw1; j.T1 = tlw1; j.R2 = -rrw1; j.T2 = trw1; }
-                    else     { j.R1 = rlw1;  j.T1 = tlw2; j.R2 = rrw1;  j.T2 = trw2; }
-                    j.dtab = filter_of(L, vel, v, sc.s.dx);
-                    j.wtab = wo;
-                    int s_ = r.first, end = r.first + r.count;
-                    int origin = d.lo(r.axis);
-                    while (s_ < end) {
-                        int e = std::min(end, (s_ / per + 1) * per);   // cut at multiples of `per`
-                        j.first = s_;
-                        j.count = e - s_;
-                        j.o1 = r.d1 >= 0 ? origin + s_ - sc.doms[r.d1].lo(r.axis) : 0;
-                        j.o2 = r.d2 >= 0 ? origin + s_ - sc.doms[r.d2].lo(r.axis) : 0;
-                        jobs.push_back(j);
-                        s_ = e;
-                    }
-                }
-            }
-        }
-        if (with_copies) {
-            for (size_t g = 0; g < gdom.size(); g++) {
-                const Domain& d = dom((int)g);
-                if (d.rigid) continue;
-                for (int ax = 0; ax < 2; ax++) {
-                    if (d.update[ax]) continue;
-                    DevJob j;
-                    std::memset(&j, 0, sizeof j);
-                    j.dom = (int)g;
-                    j.kind = JK_COPY | (ax == AX_Y ? JK_Y : 0);
-                    j.d1 = j.d2 = -1;
-                    jobs.push_back(j);
-                }
-            }
-        }
-        return jobs;
-    }
-
-    // ---------------------------------------------------------------- build
-    void build(const pstd_config* cfgs, int n_cfg) {
-        build_scenes(cfgs, n_cfg);
-        build_device();
-    }
-
-    void build_scenes(const pstd_config* cfgs, int n_cfg) {
-        if (n_cfg <= 0) throw SceneError(PSTD_ERR_INVALID, "no scenes");
-        scenes.resize(n_cfg);
-        for (int i = 0; i < n_cfg; i++) {
-            try {
-                scenes[i].build(&cfgs[i]);
-            } catch (SceneError& e) {
-                if (n_cfg == 1) throw;
-                throw SceneError(e.code, "scene " + std::to_string(i) + ": " + e.what());
-            }
-            dom_base.push_back((int)gdom.size());
-            for (size_t k = 0; k < scenes[i].doms.size(); k++) gdom.push_back({i, (int)k});
-        }
-        int nr = 0;
-        for (auto& sc : scenes) { rec_base.push_back(nr); nr += (int)sc.receivers.size(); }
-        framecount = 0;
-        for (auto& sc : scenes) framecount = std::max(framecount, sc.s.framecount());
-    }
-
-    void build_device() {
-        if (const char* e = std::getenv("PSTD_AUTOTUNE")) autotune = std::atoi(e) != 0;
-        // PSTD_VARIANT=i pins every bucket to its i-th compiled variant (tests)
-        int forced = -1;
-        if (const char* e = std::getenv("PSTD_VARIANT")) { forced = std::atoi(e); autotune = false; }
-        CK(cudaGetDevice(&device));
-        CK(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
-        CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
-
-        // ---- layout
-        auto round32 = [](long long v) { return (v + 31) / 32 * 32; };
-        long long off = 0, foff = 0, poff = 0;
-        hdoms.resize(gdom.size());
-        std::vector<float> att;
-        std::vector<int> pml_idx;
-        for (size_t k = 0; k < gdom.size(); k++) {
-            const Domain& d = dom((int)k);
-            const Scene& sc = scene_of((int)k);
-            DevDomain& h = hdoms[k];
-            std::memset(&h, 0, sizeof h);
-            h.nx = d.nx; h.ny = d.ny;
-            h.pitch_p = (int)round32(d.nx);
-            h.pitch_vx = (int)round32(d.nx + 1);
-            h.pitch_vy = (int)round32(d.nx);
-            h.fixed = d.rigid;
-            h.scene = gdom[k].first;
-            long long& o = d.rigid ? foff : off;
-            h.o_px = o; o = round32(o + (long long)h.pitch_p * d.ny);
-            h.o_py = o; o = round32(o + (long long)h.pitch_p * d.ny);
-            h.o_vx = o; o = round32(o + (long long)h.pitch_vx * d.ny);
-            h.o_vy = o; o = round32(o + (long long)h.pitch_vy * (d.ny + 1));
-            h.o_p0 = poff; poff = round32(poff + (long long)h.pitch_p * d.ny);
-            h.rho = d.rho;
-            h.c2 = sc.s.c1 * sc.s.c1;
-            float dt = sc.s.dt();
-            for (int i = 0; i < 6; i++) h.cdt[i] = dt * sc.s.rk[i];
-            h.pml = d.pml;
-            h.att_xp = h.att_xv = h.att_yp = h.att_yv = -1;
-            if (d.pml) {
-                pml_idx.push_back((int)k);
-                std::vector<double> prof;
-                if (d.att_x) {
-                    pml_profile(sc.s, false, d.asc_x, prof);
-                    h.att_xp = (int)att.size(); for (double v : prof) att.push_back((float)v);
-                    pml_profile(sc.s, true, d.asc_x, prof);
-                    h.att_xv = (int)att.size(); for (double v : prof) att.push_back((float)v);
-                }
-                if (d.att_y) {
-                    pml_profile(sc.s, false, d.asc_y, prof);
-                    h.att_yp = (int)att.size(); for (double v : prof) att.push_back((float)v);
-                    pml_profile(sc.s, true, d.asc_y, prof);
-                    h.att_yv = (int)att.size(); for (double v : prof) att.push_back((float)v);
-                }
-            }
-            if (!d.rigid) cells += (int64_t)d.nx * d.ny;
-            if (!d.pml) air_cells += (int64_t)d.nx * d.ny;
-        }
-        set_floats = (size_t)std::max<long long>(off, 32);
-        fixed_floats = (size_t)std::max<long long>(foff, 32);
-        p0_floats = (size_t)std::max<long long>(poff, 32);
-        if (att.empty()) att.push_back(1.f);
-        datt.upload(att);
-        n_pml = (int)pml_idx.size();
-        dpml.upload(pml_idx);
-        ddoms.upload(hdoms);
-
-        // ---- buckets
-        std::vector<int> Ls;
-        for (auto& sc : scenes)
-            for (const StripRun& r : sc.runs) {
-                int L = run_length(sc, r);
-                if (std::find(Ls.begin(), Ls.end(), L) == Ls.end()) Ls.push_back(L);
-            }
-        std::sort(Ls.begin(), Ls.end());
-        for (int L : Ls) {
-            const StageVariant* vs;
-            int nv = stage_variants(L, &vs);
-            if (nv <= 0)
-                throw SceneError(PSTD_ERR_UNSUPPORTED, "strip transform length " + std::to_string(L) +
-                                                           " is outside the compiled range 32..8192");
-            for (int i = 0; i < nv; i++) CK(vs[i].prepare());
-            Bucket b;
-            b.L = L;
-            int longest = 0;
-            for (auto& sc : scenes)
-                for (const StripRun& r : sc.runs)
-                    if (run_length(sc, r) == L) longest = std::max(longest, sc.doms[r.dom].len(r.axis));
-            b.rc = (longest + 2 + 3) / 4 * 4;
-            b.var = &vs[forced >= 0 ? std::min(forced, nv - 1) : 0];
-            if (b.var->smem_for(b.rc) > (size_t)smem_optin) b.var = &vs[0];   // pinned form does not fit
-            if (forced >= 0) b.choice = " pinned";
-            buckets.push_back(b);
-        }
-
-        // ---- fields: initial condition
-        for (auto& s : sets) s.alloc(set_floats);
-        init_set.alloc(set_floats);
-        fixed.alloc(fixed_floats);
-        init_fixed.alloc(fixed_floats);
-        p0.alloc(p0_floats);
-        init_p0.alloc(p0_floats);
-        first_step.alloc(scenes.size());
-        CK(cudaMemsetAsync(init_set.p, 0, set_floats * sizeof(float), stream));
-        CK(cudaMemsetAsync(init_fixed.p, 0, fixed_floats * sizeof(float), stream));
-        CK(cudaMemsetAsync(init_p0.p, 0, p0_floats * sizeof(float), stream));
-        {
-            std::vector<int> x0, y0;
-            for (size_t g = 0; g < gdom.size(); g++) { x0.push_back(dom((int)g).x0); y0.push_back(dom((int)g).y0); }
-            DevBuf<int> dx0, dy0;
-            dx0.upload(x0);
-            dy0.upload(y0);
-            for (size_t si = 0; si < scenes.size(); si++) {
-                const Scene& sc = scenes[si];
-                if (sc.speakers.empty()) continue;
-                std::vector<DevSpeaker> spk;
-                for (auto& q : sc.speakers) spk.push_back({q.x, q.y});
-                DevBuf<DevSpeaker> dspk;
-                dspk.upload(spk);
-                const int b = dom_base[si];
-                CK(launch_speakers(ddoms.p + b, dx0.p + b, dy0.p + b, (int)sc.doms.size(), dspk.p, (int)spk.size(),
-                                   sc.s.dx, sc.s.band_width, init_set.p, init_fixed.p, init_p0.p, stream));
-                CK(cudaStreamSynchronize(stream));
-            }
-        }
-
-        // ---- receivers, frames
-        std::vector<DevReceiver> rec;
-        for (size_t si = 0; si < scenes.size(); si++)
-            for (auto& r : scenes[si].receivers) rec.push_back({dom_base[si] + r.dom, r.row, r.col});
-        n_rec = (int)rec.size();
-        drec.upload(rec);
-        ring_cap = std::max(framecount, 1);
-        dring.alloc((size_t)ring_cap * std::max(n_rec, 1));
-        dcounter.alloc(1);
-        frame_floats = 0;
-        for (size_t k = 0; k < gdom.size(); k++) {
-            if (dom((int)k).pml) continue;
-            frame_doms.push_back((int)k);
-            frame_off.push_back((long long)frame_floats);
-            frame_floats += (size_t)dom((int)k).nx * dom((int)k).ny;
-        }
-        dframe_doms.upload(frame_doms);
-        dframe_off.upload(frame_off);
-        dframe.alloc(std::max<size_t>(frame_floats, 1));
-
-        // ---- tables and the job plan (autotuned)
-        reset();
-        plan(autotune);
-        reset();
-        for (size_t i = 0; i < buckets.size(); i++) {
-            cudaStream_t s;
-            CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
-            side.push_back(s);
-        }
-        capture_graphs();
-        std::string choice;
-        for (auto& b : buckets) choice += " [" + std::string(b.var->name) + b.choice + "]";
-        log(PSTD_LOG_DEBUG, std::to_string(scenes.size()) + " scene(s), " + std::to_string(gdom.size()) + " domains, " +
-                                std::to_string(n_rec) + " receivers; stage kernels:" + choice);
-    }
-
-    StageArgs stage_args(int c, int k, const DevJob* jobs, const float2* twp, int fp, int fv, int rc) {
-        const int A = (c + 1) % 3, B = (c + 2) % 3;
-        StageArgs a;
-        a.jobs = jobs;
-        a.doms = ddoms.p;
-        a.in = sets[k == 0 ? c : ((k - 1) % 2 == 0 ? A : B)].p;
-        a.prev = sets[c].p;
-        a.out = sets[k % 2 == 0 ? A : B].p;
-        a.fixed = fixed.p;
-        a.p0 = p0.p;
-        a.first_step = first_step.p;
-        a.filt = dfilt.p;
-        a.filt_p = dfilt.p + fp;
-        a.filt_v = dfilt.p + fv;
-        a.win = dwin.p;
-        a.tw = twp;
-        a.att = datt.p;
-        a.stage = k;
-        a.last = k == 5;
-        a.row_cap = rc;
-        return a;
-    }
-
-    void upload_tables() {
-        dfilt.upload(filt);
-        dtw.upload(tw);
-        dwin.upload(win);
-    }
-
-    // the persistent form stages one pressure / velocity filter pair per CTA
-    static bool one_filter_pair(const std::vector<DevJob>& jobs, int fp, int fv) {
-        for (const DevJob& j : jobs)
-            if (!(j.kind & JK_COPY) && j.dtab != ((j.kind & JK_VEL) ? fv : fp)) return false;
-        return true;
-    }
-
-    // choose a variant per bucket by timing each on this batch's jobs
-    void plan(bool tune) {
-        if (tune) {
-            for (auto& b : buckets) {
-                const StageVariant* vs;
-                int nv = stage_variants(b.L, &vs);
-                if (nv <= 1) continue;
-                std::vector<std::vector<DevJob>> all(nv);
-                std::vector<int> twv(nv), fpv(nv), fvv(nv);
-                for (int i = 0; i < nv; i++) {
-                    all[i] = make_jobs(b.L, &vs[i], false);
-                    twv[i] = twiddles_of(&vs[i]);
-                    fpv[i] = filter_of(b.L, false, &vs[i], scenes[0].s.dx);
-                    fvv[i] = filter_of(b.L, true, &vs[i], scenes[0].s.dx);
-                    if (vs[i].persistent && !one_filter_pair(all[i], fpv[i], fvv[i])) all[i].clear();
-                    if (vs[i].smem_for(b.rc) > (size_t)smem_optin) all[i].clear();   // staging too large
-                }
-                upload_tables();
-                float best = 1e30f;
-                int best_i = 0;
-                std::string rec;
-                cudaEvent_t e0, e1;
-                CK(cudaEventCreate(&e0));
-                CK(cudaEventCreate(&e1));
-                for (int i = 0; i < nv; i++) {
-                    if (all[i].empty()) continue;
-                    DevBuf<DevJob> tj;
-                    tj.upload(all[i]);
-                    StageArgs a = stage_args(cur, 1, tj.p, dtw.p + twv[i], fpv[i], fvv[i], b.rc);
-                    if (vs[i].launch((int)all[i].size(), a, stream) != cudaSuccess) {
-                        cudaGetLastError();   // this variant's staging does not fit the bucket's strips
-                        rec += " " + std::to_string(i) + ":n/a";
-                        continue;
-                    }
-                    CK(vs[i].launch((int)all[i].size(), a, stream));
-                    CK(cudaEventRecord(e0, stream));
-                    const int reps = 5;
-                    for (int w = 0; w < reps; w++) CK(vs[i].launch((int)all[i].size(), a, stream));
-                    CK(cudaEventRecord(e1, stream));
-                    CK(cudaEventSynchronize(e1));
-                    float ms;
-                    CK(cudaEventElapsedTime(&ms, e0, e1));
-                    ms /= reps;
-                    char buf[64];
-                    std::snprintf(buf, sizeof buf, " %d:%.1fus", i, ms * 1e3f);
-                    rec += buf;
-                    if (ms < best) { best = ms; best_i = i; }
-                }
-                cudaEventDestroy(e0);
-                cudaEventDestroy(e1);
-                b.var = &vs[best_i];
-                b.choice = " tuned" + rec;
-            }
-        }
-        std::vector<DevJob> jobs;
-        for (size_t i = 0; i < buckets.size(); i++) {
-            auto& b = buckets[i];
-            auto js = make_jobs(b.L, b.var, i + 1 == buckets.size());
-            b.tw_off = twiddles_of(b.var);
-            b.fp_off = filter_of(b.L, false, b.var, scenes[0].s.dx);
-            b.fv_off = filter_of(b.L, true, b.var, scenes[0].s.dx);
-            if (b.var->persistent && !one_filter_pair(js, b.fp_off, b.fv_off)) {
-                // mixed grid spacings: fall back to the first plain variant
-                const StageVariant* vs;
-                int nv = stage_variants(b.L, &vs);
-                for (int q = 0; q < nv; q++) if (!vs[q].persistent) { b.var = &vs[q]; break; }
-                js = make_jobs(b.L, b.var, i + 1 == buckets.size());
-                b.tw_off = twiddles_of(b.var);
-                b.choice += " (plain: several grid spacings)";
-            }
-            b.off = (int)jobs.size();
-            b.n = (int)js.size();
-            jobs.insert(jobs.end(), js.begin(), js.end());
-        }
-        upload_tables();
-        djobs.upload(jobs);
-    }
-
-    void reset() {
-        for (auto& s : sets) CK(cudaMemsetAsync(s.p, 0, set_floats * sizeof(float), stream));
-        CK(cudaMemcpyAsync(sets[0].p, init_set.p, set_floats * sizeof(float), cudaMemcpyDeviceToDevice, stream));
-        CK(cudaMemcpyAsync(fixed.p, init_fixed.p, fixed_floats * sizeof(float), cudaMemcpyDeviceToDevice, stream));
-        CK(cudaMemcpyAsync(p0.p, init_p0.p, p0_floats * sizeof(float), cudaMemcpyDeviceToDevice, stream));
-        std::vector<int> ones(scenes.size(), 1);
-        CK(cudaMemcpy(first_step.p, ones.data(), ones.size() * sizeof(int), cudaMemcpyHostToDevice));
-        CK(cudaMemsetAsync(dcounter.p, 0, sizeof(int), stream));
-        CK(cudaStreamSynchronize(stream));
-        cur = 0;
-        steps = 0;
-    }
-
-    int launches_per_step() const { return 6 * (int)buckets.size() + (n_pml > 0) + 1; }
-
-    // Enqueue one time step from set `c` on `st`.  concurrent: the buckets of
-    // a stage go on side streams (fork/join); ev (optional): events around
-    // each stage's launches, which then run back to back on `st`.
-    void enqueue_step(int c, cudaStream_t st, bool concurrent,
-                      std::vector<std::pair<cudaEvent_t, cudaEvent_t>>* ev = nullptr) {
-        const int B = (c + 2) % 3;
-        std::vector<cudaEvent_t> tmp;
-        auto mk = [&]() {
-            cudaEvent_t e;
-            CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-            tmp.push_back(e);
-            return e;
-        };
-        for (int k = 0; k < 6; k++) {
-            cudaEvent_t t0 = nullptr, t1 = nullptr;
-            if (ev) {
-                CK(cudaEventCreate(&t0));
-                CK(cudaEventCreate(&t1));
-                CK(cudaEventRecord(t0, st));
-            }
-            if (concurrent && buckets.size() > 1) {
-                cudaEvent_t fork = mk();
-                CK(cudaEventRecord(fork, st));
-                std::vector<cudaEvent_t> joins;
-                for (size_t i = 0; i < buckets.size(); i++) {
-                    auto& b = buckets[i];
-                    cudaStream_t s = i == 0 ? st : side[i];
-                    if (i > 0) CK(cudaStreamWaitEvent(s, fork, 0));
-                    StageArgs a = stage_args(c, k, djobs.p + b.off, dtw.p + b.tw_off, b.fp_off, b.fv_off, b.rc);
-                    CK(b.var->launch(b.n, a, s));
-                    if (i > 0) {
-                        cudaEvent_t j = mk();
-                        CK(cudaEventRecord(j, s));
-                        joins.push_back(j);
-                    }
-                }
-                for (auto j : joins) CK(cudaStreamWaitEvent(st, j, 0));
-            } else {
-                for (auto& b : buckets) {
-                    StageArgs a = stage_args(c, k, djobs.p + b.off, dtw.p + b.tw_off, b.fp_off, b.fv_off, b.rc);
-                    CK(b.var->launch(b.n, a, st));
-                }
-            }
-            if (ev) {
-                CK(cudaEventRecord(t1, st));
-                ev->push_back({t0, t1});
-            }
-        }
-        if (n_pml > 0) CK(launch_pml_post(dpml.p, n_pml, ddoms.p, sets[B].p, fixed.p, p0.p, datt.p, st));
-        CK(cudaMemsetAsync(first_step.p, 0, scenes.size() * sizeof(int), st));
-        CK(launch_receivers(drec.p, n_rec, ddoms.p, sets[B].p, dring.p, ring_cap, dcounter.p, st));
-        for (auto e : tmp) cudaEventDestroy(e);   // destruction is deferred until the event completes
-    }
-
-    void capture_graphs() {
-        graphs_ok = false;
-        bool ok = true;
-        for (int c = 0; c < 3 && ok; c++) {
-            cudaGraph_t g = nullptr;
-            if (cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) { ok = false; break; }
-            try {
-                enqueue_step(c, stream, true);
-            } catch (...) {
-                cudaStreamEndCapture(stream, &g);
-                if (g) cudaGraphDestroy(g);
-                ok = false;
-                break;
-            }
-            if (cudaStreamEndCapture(stream, &g) != cudaSuccess || !g) { ok = false; break; }
-            if (cudaGraphInstantiate(&graphs[c], g, 0) != cudaSuccess) { cudaGraphDestroy(g); ok = false; break; }
-            cudaGraphDestroy(g);
-        }
-        cudaGetLastError();
-        graphs_ok = ok;
-        if (!ok) log(PSTD_LOG_WARNING, "CUDA graph capture failed; launching kernels directly");
-    }
-
-    void step(cudaStream_t st) {
-        if (graphs_ok) CK(cudaGraphLaunch(graphs[cur], st));
-        else enqueue_step(cur, st, false);
-        cur = (cur + 2) % 3;
-        steps++;
-    }
-};
 
 static int run_frames(Kernel* k, const pstd_callbacks* cb) {
     if (k->scenes.size() != 1) throw SceneError(PSTD_ERR_INVALID, "run() delivers frames of a single scene; advance batches");
