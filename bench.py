@@ -54,6 +54,10 @@ def workload(name: str, seed: int):
                                                   "alpha 0.3 + 50-cell PML edges, 4 speakers, 16 receivers")
     if name == "square":
         return scenes.plain_square(seed), "square 200x200 cells + 50-cell PML, 1 speaker, 4 receivers"
+    if name == "large":
+        return scenes.large_square(seed, half=4096, steps=1000), (
+            "8192x8192 cells as 2x2 domains of 4096x4096 with windowed interfaces, 50-cell PML (alpha 1) on the "
+            "outer edges, 2 speakers, 64 receivers")
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -388,7 +392,7 @@ def run_ours(args):
                 "plan": k.plan_info().strip().splitlines()}
 
     # ---- end-to-end through the reference-facing API (host callbacks)
-    e2e_steps = min(args.steps, 400)
+    e2e_steps = min(args.steps, 400, max(5, int(4e8 // cells)))   # every frame goes to the host
     ce = conf.copy()
     dt = ce.Settings.GetTimeStep()
     ce.Settings.SetRenderTime(float(np.float32((e2e_steps + 0.5) * float(dt))))
