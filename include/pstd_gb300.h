@@ -131,6 +131,14 @@ int pstd_get_metadata(pstd_kernel* k, int32_t* n_domains, int32_t* dims, int32_t
  * calling thread; callbacks run on it, in frame order. */
 int pstd_run(pstd_kernel* k, const pstd_callbacks* cb);
 
+/* pstd_run with frame subsampling on the device (no reference counterpart):
+ * frames every save_nth-th step (0 = the scene's SaveNth, kernel/Solver.cpp:80)
+ * and, for stride > 1, only every stride-th row and column of each domain, so
+ * write_frame gets ceil(Nx/stride) * ceil(Ny/stride) floats, row-major.
+ * Cuts the device-to-host traffic of runs that do not need every frame at
+ * full resolution; receiver samples are unchanged. */
+int pstd_run_sub(pstd_kernel* k, const pstd_callbacks* cb, int32_t save_nth, int32_t stride);
+
 /* ---- device-resident stepping (no reference counterpart) --------------- */
 /* Advance n_steps time steps on `stream` (a cudaStream_t, NULL = the handle's
  * own stream) without callbacks.  Receiver samples are kept on the device

@@ -46,6 +46,7 @@ SIGNATURES = {
     "pstd_destroy": (None, [_vp]),
     "pstd_get_metadata": (ctypes.c_int, [_vp, _P(_i32), _P(_i32), _i32, _P(_i32)]),
     "pstd_run": (ctypes.c_int, [_vp, _P(c_callbacks)]),
+    "pstd_run_sub": (ctypes.c_int, [_vp, _P(c_callbacks), _i32, _i32]),
     "pstd_advance": (ctypes.c_int, [_vp, _i32, _vp]),
     "pstd_reset": (ctypes.c_int, [_vp]),
     "pstd_synchronize": (ctypes.c_int, [_vp]),

@@ -191,6 +191,55 @@ class PSTDConfiguration:
         import copy
         return copy.deepcopy(self)
 
+    # ---- scene files: the PSTDConfiguration fields as JSON (Python floats
+    # are written with enough digits to round-trip exactly)
+    _SETTINGS = ["calctime", "c1", "ampMax", "freqMax", "rho", "patcherror", "tfactRK", "gridSpacing", "band_width",
+                 "wave_length"]
+
+    def to_dict(self) -> dict:
+        s = self.Settings
+        edge = lambda e: {"Absorption": float(e.Absorption), "LR": bool(e.LR)}
+        return {
+            "Settings": {**{k: float(getattr(s, k)) for k in self._SETTINGS},
+                         "rk_coefficients": [float(x) for x in s.rk_coefficients],
+                         "spectral_interpolation": bool(s.spectral_interpolation),
+                         "PMLCells": int(s.PMLCells), "SaveNth": int(s.SaveNth)},
+            "Domains": [{"TopLeft": [float(d.TopLeft[0]), float(d.TopLeft[1])],
+                         "Size": [float(d.Size[0]), float(d.Size[1])],
+                         "T": edge(d.T), "L": edge(d.L), "B": edge(d.B), "R": edge(d.R)} for d in self.Domains],
+            "Speakers": [[float(v) for v in p] for p in self.Speakers],
+            "Receivers": [[float(v) for v in p] for p in self.Receivers],
+        }
+
+    @staticmethod
+    def from_dict(d: dict) -> "PSTDConfiguration":
+        conf = PSTDConfiguration()
+        s, src = conf.Settings, d["Settings"]
+        for k in PSTDConfiguration._SETTINGS:
+            setattr(s, k, f32(src[k]))
+        s.rk_coefficients = [float(x) for x in src["rk_coefficients"]]
+        s.spectral_interpolation = bool(src.get("spectral_interpolation", False))
+        s.PMLCells = int(src["PMLCells"])
+        s.SaveNth = int(src["SaveNth"])
+        edge = lambda e: DomainConfEdge(float(e["Absorption"]), bool(e["LR"]))
+        conf.Domains = [DomainConf((float(x["TopLeft"][0]), float(x["TopLeft"][1])),
+                                   (float(x["Size"][0]), float(x["Size"][1])),
+                                   edge(x["T"]), edge(x["L"]), edge(x["B"]), edge(x["R"])) for x in d["Domains"]]
+        conf.Speakers = [tuple(float(v) for v in p) for p in d["Speakers"]]
+        conf.Receivers = [tuple(float(v) for v in p) for p in d["Receivers"]]
+        return conf
+
+    def save(self, path: str):
+        import json
+        with open(path, "w") as f:
+            json.dump(self.to_dict(), f, indent=1)
+
+    @staticmethod
+    def load(path: str) -> "PSTDConfiguration":
+        import json
+        with open(path) as f:
+            return PSTDConfiguration.from_dict(json.load(f))
+
 
 # ---------------------------------------------------------------------------
 # ctypes mirror of include/pstd_gb300.h

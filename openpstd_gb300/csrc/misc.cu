@@ -117,14 +117,16 @@ __global__ void server_receiver_kernel(const DevSrvReceiver* rec, int n_rec, con
     for (int i = threadIdx.x; i < n_slots; i += blockDim.x) scene_step[slots[i]] += 1;
 }
 
+// p0 = px + py of every `sub`-th row and column (sub = 1: the whole domain)
 __global__ void frame_kernel(const int* idx, const long long* dst_off, const DevDomain* doms,
-                             const float* __restrict__ set, float* dst) {
+                             const float* __restrict__ set, float* dst, int sub) {
     const DevDomain d = doms[idx[blockIdx.y]];
     float* out = dst + dst_off[blockIdx.y];
+    const int mx = (d.nx + sub - 1) / sub, my = (d.ny + sub - 1) / sub;
     const int stride = gridDim.x * blockDim.x;
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < d.nx * d.ny; k += stride) {
-        const int r = k / d.nx, i = k - r * d.nx;
-        const long long e = (long long)r * d.pitch_p + i;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < mx * my; k += stride) {
+        const int r = k / mx, i = k - r * mx;
+        const long long e = (long long)r * sub * d.pitch_p + (long long)i * sub;
         out[k] = __fadd_rn(set[d.o_px + e], set[d.o_py + e]);
     }
 }
@@ -157,9 +159,9 @@ cudaError_t launch_server_receivers(const DevSrvReceiver* rec, int n_rec, const 
 }
 
 cudaError_t launch_frame(const int* idx, const long long* dst_off, int n, const DevDomain* doms, const float* set,
-                         float* dst, cudaStream_t st) {
+                         float* dst, cudaStream_t st, int sub) {
     if (n <= 0) return cudaSuccess;
-    frame_kernel<<<dim3(64, n), 256, 0, st>>>(idx, dst_off, doms, set, dst);
+    frame_kernel<<<dim3(64, n), 256, 0, st>>>(idx, dst_off, doms, set, dst, sub);
     return cudaGetLastError();
 }
 

@@ -42,12 +42,26 @@ int set_error(int code, const std::string& message) {
 }
 
 
-static int run_frames(Kernel* k, const pstd_callbacks* cb) {
+// save_nth > 0 overrides the scene's SaveNth; sub > 1 subsamples every frame
+// on the device (every sub-th row and column) before it is copied out
+static int run_frames(Kernel* k, const pstd_callbacks* cb, int save_nth = 0, int sub = 1) {
     if (k->scenes.size() != 1) throw SceneError(PSTD_ERR_INVALID, "run() delivers frames of a single scene; advance batches");
     const Scene& sc = k->scenes[0];
     const int nframes = k->framecount;
-    const int save = std::max(1, sc.s.save_nth);
-    const size_t frame_floats = k->frame_floats;
+    const int save = save_nth > 0 ? save_nth : std::max(1, sc.s.save_nth);
+    sub = std::max(1, sub);
+    std::vector<long long> foff(k->frame_doms.size());
+    std::vector<size_t> fn(k->frame_doms.size());
+    size_t frame_floats = 0;
+    for (size_t i = 0; i < k->frame_doms.size(); i++) {
+        const DevDomain& d = k->hdoms[k->frame_doms[i]];
+        foff[i] = (long long)frame_floats;
+        fn[i] = (size_t)((d.nx + sub - 1) / sub) * (size_t)((d.ny + sub - 1) / sub);
+        frame_floats += fn[i];
+    }
+    DevBuf<long long> dsub_off;
+    if (sub > 1) dsub_off.upload(foff);
+    const long long* doff = sub > 1 ? dsub_off.p : k->dframe_off.p;
     const int K = 3;   // frames in flight
     const size_t slot = frame_floats + (size_t)std::max(k->n_rec, 1);
     PinnedBuf stage;
@@ -63,9 +77,8 @@ static int run_frames(Kernel* k, const pstd_callbacks* cb) {
         float* base = stage.p + slot * p.slot;
         for (size_t i = 0; i < k->frame_doms.size(); i++) {
             int d = k->frame_doms[i];
-            size_t n = (size_t)k->hdoms[d].nx * k->hdoms[d].ny;
             if (cb && cb->write_frame && status == PSTD_OK)
-                if (cb->write_frame(cb->user, p.frame, sc.doms[d].id, base + k->frame_off[i], (int64_t)n) != 0)
+                if (cb->write_frame(cb->user, p.frame, sc.doms[d].id, base + foff[i], (int64_t)fn[i]) != 0)
                     status = PSTD_ERR_CALLBACK;
         }
         for (int r = 0; r < k->n_rec; r++) {
@@ -86,8 +99,8 @@ static int run_frames(Kernel* k, const pstd_callbacks* cb) {
             next_slot = (next_slot + 1) % K;
             float* base = stage.p + slot * s;
             if (frame_floats) {
-                CK(launch_frame(k->dframe_doms.p, k->dframe_off.p, (int)k->frame_doms.size(), k->ddoms.p,
-                                k->sets[k->cur].p, k->dframe.p, k->stream));
+                CK(launch_frame(k->dframe_doms.p, doff, (int)k->frame_doms.size(), k->ddoms.p, k->sets[k->cur].p,
+                                k->dframe.p, k->stream, sub));
                 CK(cudaMemcpyAsync(base, k->dframe.p, frame_floats * sizeof(float), cudaMemcpyDeviceToHost, k->stream));
             }
             if (k->n_rec > 0) {
@@ -232,6 +245,12 @@ int pstd_get_metadata(pstd_kernel* h, int32_t* n_domains, int32_t* dims, int32_t
 int pstd_run(pstd_kernel* h, const pstd_callbacks* cb) {
     NEED_DEVICE(h);
     GUARD({ return run_frames(h->k.get(), cb); })
+}
+
+int pstd_run_sub(pstd_kernel* h, const pstd_callbacks* cb, int32_t save_nth, int32_t stride) {
+    NEED_DEVICE(h);
+    if (save_nth < 0 || stride < 1) return fail(PSTD_ERR_INVALID, "save_nth must be >= 0 and stride >= 1");
+    GUARD({ return run_frames(h->k.get(), cb, save_nth, stride); })
 }
 
 int pstd_advance(pstd_kernel* h, int32_t n_steps, void* stream) {

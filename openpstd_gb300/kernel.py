@@ -118,7 +118,12 @@ class PSTDKernel(KernelInterface):
         self._h = h
         self._keep = [logcb, cbs]
 
-    def run(self, callback: KernelCallback):
+    def run(self, callback: KernelCallback, save_nth: int = 0, stride: int = 1):
+        """Run Framecount steps with WriteFrame / WriteSample callbacks.
+
+        ``save_nth`` (> 0) overrides the scene's SaveNth; ``stride`` > 1
+        subsamples every frame on the device (every stride-th row and column)
+        before it is copied to the host (pstd_run_sub)."""
         h = self._need()
         errors = []
 
@@ -140,7 +145,10 @@ class PSTDKernel(KernelInterface):
 
         fcb, scb, lcb = _lib.WRITE_FRAME(_frame), _lib.WRITE_SAMPLE(_sample), _log_bridge(callback)
         cbs = _lib.c_callbacks(None, fcb, scb, lcb)
-        rc = _lib.lib().pstd_run(h, ctypes.byref(cbs))
+        if save_nth or stride != 1:
+            rc = _lib.lib().pstd_run_sub(h, ctypes.byref(cbs), int(save_nth), int(stride))
+        else:
+            rc = _lib.lib().pstd_run(h, ctypes.byref(cbs))
         if errors:
             raise errors[0]
         _lib.check(rc)
