@@ -90,6 +90,20 @@ static std::vector<int> bin_positions(int L, const int* r, int np) {
     return pos;
 }
 
+// PSTD_DFT=bf16x3 selects the split-BF16 tensor-core DFT variants for the
+// strip lengths that have one (precision study); the default is FP32
+inline bool want_bf16_dft() {
+    const char* e = std::getenv("PSTD_DFT");
+    return e && std::string(e) == "bf16x3";
+}
+
+// the FP32 variants come first in every list; the study variants follow
+inline int fp32_variants(const StageVariant* vs, int nv) {
+    int n = 0;
+    while (n < nv && !vs[n].bf16) n++;
+    return n;
+}
+
 struct Bucket {
     int L = 0;
     const StageVariant* var = nullptr;
@@ -432,8 +446,12 @@ struct Kernel {
                 for (const StripRun& r : sc.runs)
                     if (run_length(sc, r) == L) longest = std::max(longest, sc.doms[r.dom].len(r.axis));
             b.rc = (longest + 2 + 3) / 4 * 4;
-            b.var = &vs[forced >= 0 ? std::min(forced, nv - 1) : 0];
+            const int nv_fp32 = fp32_variants(vs, nv);
+            b.var = &vs[forced >= 0 ? std::min(forced, nv_fp32 - 1) : 0];
             if (b.var->smem_for(b.rc) > (size_t)smem_optin) b.var = &vs[0];   // pinned form does not fit
+            if (want_bf16_dft())
+                for (int i = 0; i < nv; i++)
+                    if (vs[i].bf16) { b.var = &vs[i]; b.choice = " split-BF16 DFT (precision study)"; }
             if (forced >= 0) b.choice = " pinned";
             buckets.push_back(b);
         }
@@ -548,6 +566,7 @@ struct Kernel {
             for (size_t bi = 0; bi < buckets.size(); bi++) {
                 auto& b = buckets[bi];
                 if (tune_only && !(*tune_only)[bi]) continue;
+                if (b.var->bf16) continue;   // the precision-study form is chosen, not tuned
                 const StageVariant* vs;
                 int nv = stage_variants(b.L, &vs);
                 if (nv <= 1) continue;
@@ -560,6 +579,7 @@ struct Kernel {
                     fvv[i] = filter_of(b.L, true, &vs[i], scenes[0].s.dx);
                     if (vs[i].persistent && !one_filter_pair(all[i], fpv[i], fvv[i])) all[i].clear();
                     if (vs[i].smem_for(b.rc) > (size_t)smem_optin) all[i].clear();   // staging too large
+                    if (vs[i].bf16) all[i].clear();                                  // different arithmetic
                 }
                 upload_tables();
                 float best = 1e30f;

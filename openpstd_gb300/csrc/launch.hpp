@@ -33,6 +33,7 @@ struct StageVariant {
     int r[4];                                                   // radix of each pass
     bool persistent;                                            // warp-specialised persistent form
     bool pipe;                                                  // pipelined persistent form (cp.async staging)
+    bool bf16;                                                  // split-BF16 tensor-core DFT (precision study, opt-in)
     cudaError_t (*launch)(int n_jobs, const StageArgs& a, cudaStream_t st);
     cudaError_t (*prepare)();
     size_t (*smem_for)(int row_cap);                            // dynamic shared memory of one CTA

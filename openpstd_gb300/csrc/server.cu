@@ -324,7 +324,7 @@ struct Server {
             b.rc = (longest + 2 + 3) / 4 * 4;
             bool need = false;
             if (forced >= 0) {
-                b.var = &vs[std::min(forced, nv - 1)];
+                b.var = &vs[std::min(forced, fp32_variants(vs, nv) - 1)];
                 b.choice = " pinned";
             } else if (var_cache.count(L)) {
                 b.var = var_cache[L];

@@ -39,7 +39,10 @@
 // arithmetic: the filter is Hermitian, so the operator is real and acts on
 // the real and imaginary parts separately.
 #pragma once
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
+
+#include <cstdint>
 
 #include "launch.hpp"
 
@@ -141,9 +144,10 @@ struct DFT<16, INV> {
 // ---------------------------------------------------------------- variants
 // Plain form: L, complex strips per CTA, threads, min CTAs per SM, radices.
 // Persistent form (NTP > 0): NT FFT threads + NTP memory threads.
-template <int L_, int CS_, int NT_, int MINB_, int R0_, int R1_, int R2_ = 0, int R3_ = 0, int NTP_ = 0>
+// TC = 1: radix-16 passes as split-BF16 tensor-core GEMMs (precision study).
+template <int L_, int CS_, int NT_, int MINB_, int R0_, int R1_, int R2_ = 0, int R3_ = 0, int NTP_ = 0, int TC_ = 0>
 struct Cfg {
-    static constexpr int L = L_, CS = CS_, NT = NT_, MINB = MINB_, NTP = NTP_;
+    static constexpr int L = L_, CS = CS_, NT = NT_, MINB = MINB_, NTP = NTP_, TC = TC_;
     static constexpr int R0 = R0_, R1 = R1_, R2 = R2_, R3 = R3_;
     static constexpr int NP = R3_ ? 4 : (R2_ ? 3 : 2);
     static_assert(R0 * R1 * (R2 ? R2 : 1) * (R3 ? R3 : 1) == L, "radix plan must multiply to L");
@@ -187,8 +191,233 @@ __device__ __forceinline__ void load_twiddles(const float2* row, float2 (&w)[R])
     }
 }
 
+// ---------------------------------------------------------------- split-BF16 DFT-16 on tensor cores
+// Precision study for long strips (an opt-in variant, never picked by the
+// autotuner): sixteen radix-16 butterflies of a pass form the rows of a real
+// GEMM  [Re x | Im x] (16 x 32) * F (32 x 32) = [Re y | Im y]  with
+// F = [[C, -S], [S, C]], C = cos(2 pi q k / 16), S = sin(...) for the
+// forward transform (the inverse flips the sign of the S blocks).  Every
+// operand is split into bf16 hi + lo (x = hi + lo to about 2^-17), and the
+// product is accumulated in fp32 as lo*hi + hi*lo + hi*hi (lo*lo dropped) on
+// mma.sync m16n8k16 (row.col, bf16 -> f32).  Lane (g = lane / 4, t = lane % 4)
+// holds two butterflies (rows g and g + 8) at the positions {2t, 2t+1, 2t+8,
+// 2t+9}; the accumulator layout of m16n8 equals the A layout of the next
+// product, so forward DFT -> filter -> inverse DFT stays in registers.
+
+__device__ __forceinline__ float cos16(int m) {   // cos(2 pi m / 16)
+    switch (m & 15) {
+        case 0: return 1.f;
+        case 1: case 15: return PSTD_C8;
+        case 2: case 14: return PSTD_R2;
+        case 3: case 13: return PSTD_S8;
+        case 4: case 12: return 0.f;
+        case 5: case 11: return -PSTD_S8;
+        case 6: case 10: return -PSTD_R2;
+        case 7: case 9: return -PSTD_C8;
+        default: return -1.f;
+    }
+}
+__device__ __forceinline__ float sin16(int m) { return cos16(m - 4); }   // sin(x) = cos(x - pi/2)
+
+__device__ __forceinline__ void split_pack(float a, float b, uint32_t& hi, uint32_t& lo) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);   // a in the low half (lower column)
+    const float2 hf = __bfloat1622float2(h);
+    const __nv_bfloat162 l = __floats2bfloat162_rn(a - hf.x, b - hf.y);
+    hi = *reinterpret_cast<const uint32_t*>(&h);
+    lo = *reinterpret_cast<const uint32_t*>(&l);
+}
+
+// B fragments of the forward matrix: [kk][nt][reg], k = kk*16 + 2t + 8*reg (+1), n = nt*8 + g
+struct TCFrag {
+    uint32_t hi[2][4][2], lo[2][4][2];
+};
+
+__device__ __forceinline__ float dft_entry_fwd(int k, int n) {
+    const int m = ((k & 15) * (n & 15)) & 15;
+    const bool xi = k >= 16, yi = n >= 16;
+    if (xi == yi) return cos16(m);
+    return xi ? sin16(m) : -sin16(m);
+}
+
+__device__ __forceinline__ void tc_matrix(TCFrag& F, int lane) {
+    const int g = lane >> 2, t = lane & 3;
+#pragma unroll
+    for (int kk = 0; kk < 2; kk++)
+#pragma unroll
+        for (int nt = 0; nt < 4; nt++)
+#pragma unroll
+            for (int r = 0; r < 2; r++) {
+                const int k = kk * 16 + 2 * t + 8 * r, n = nt * 8 + g;
+                split_pack(dft_entry_fwd(k, n), dft_entry_fwd(k + 1, n), F.hi[kk][nt][r], F.lo[kk][nt][r]);
+            }
+}
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+        "{%0, %1, %2, %3};"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// positions of the lane's four values within a butterfly: 2t, 2t+1, 2t+8, 2t+9
+__device__ __forceinline__ int tc_pos(int t, int j) { return 2 * t + (j & 1) + ((j >> 1) << 3); }
+
+// y = DFT16(x) (INV: inverse, unnormalised) for the lane's two butterflies
+template <bool INV>
+__device__ __forceinline__ void tc_dft(const float2 (&x)[2][4], float2 (&y)[2][4], const TCFrag& F) {
+    uint32_t ah[2][4], al[2][4];
+#pragma unroll
+    for (int kk = 0; kk < 2; kk++) {
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            // a regs: 0 (row g, cols 2t..), 1 (row g+8), 2 (row g, cols 2t+8..), 3 (row g+8, cols 2t+8..)
+            const int i = r & 1, j = (r >> 1) * 2;
+            const float2 u = x[i][j], v = x[i][j + 1];
+            split_pack(kk ? u.y : u.x, kk ? v.y : v.x, ah[kk][r], al[kk][r]);
+        }
+    }
+    float d[4][4];
+#pragma unroll
+    for (int nt = 0; nt < 4; nt++) {
+#pragma unroll
+        for (int e = 0; e < 4; e++) d[nt][e] = 0.f;
+#pragma unroll
+        for (int kk = 0; kk < 2; kk++) {
+            // the inverse matrix flips the sign of the blocks that map Re <-> Im
+            const uint32_t flip = (INV && ((kk == 0) == (nt >= 2))) ? 0x80008000u : 0u;
+            const uint32_t bh0 = F.hi[kk][nt][0] ^ flip, bh1 = F.hi[kk][nt][1] ^ flip;
+            const uint32_t bl0 = F.lo[kk][nt][0] ^ flip, bl1 = F.lo[kk][nt][1] ^ flip;
+            mma_bf16(d[nt], al[kk], bh0, bh1);
+            mma_bf16(d[nt], ah[kk], bl0, bl1);
+            mma_bf16(d[nt], ah[kk], bh0, bh1);
+        }
+    }
+    // d[nt][0..1]: row g, columns nt*8 + 2t + {0,1}; d[nt][2..3]: row g + 8
+#pragma unroll
+    for (int i = 0; i < 2; i++) {
+        y[i][0] = make_float2(d[0][2 * i], d[2][2 * i]);
+        y[i][1] = make_float2(d[0][2 * i + 1], d[2][2 * i + 1]);
+        y[i][2] = make_float2(d[1][2 * i], d[3][2 * i]);
+        y[i][3] = make_float2(d[1][2 * i + 1], d[3][2 * i + 1]);
+    }
+}
+
+// forward (DIF) radix-16 pass of block size M: DFT then twiddle
+template <class C, int M, int TOFF, int NTH, bool SMT>
+__device__ __forceinline__ void fwd_pass_tc(float2* sm, const float2* tw, int tid) {
+    constexpr int Q = M / 16, GROUPS = C::CS * (C::L / 16) / 16, NW = NTH / 32;
+    const int lane = tid & 31, g = lane >> 2, t = lane & 3;
+    TCFrag F;
+    tc_matrix(F, lane);
+    for (int grp = tid >> 5; grp < GROUPS; grp += NW) {
+        float2* base[2];
+        int n1s[2];
+        float2 x[2][4], y[2][4];
+#pragma unroll
+        for (int i = 0; i < 2; i++) {
+            const int it = grp * 16 + g + 8 * i;
+            const int cs = it % C::CS, b = it / C::CS;
+            n1s[i] = b % Q;
+            base[i] = sm + cs * C::SP + (b / Q) * M + n1s[i];
+#pragma unroll
+            for (int j = 0; j < 4; j++) x[i][j] = base[i][tc_pos(t, j) * Q];
+        }
+        tc_dft<false>(x, y, F);
+#pragma unroll
+        for (int i = 0; i < 2; i++) {
+            if (Q > 1) {
+                const float4* w4 = reinterpret_cast<const float4*>(tw + TOFF + n1s[i] * 16 + 2 * t);
+                const float4 w0 = tload<SMT>(w4), w1 = tload<SMT>(w4 + 4);   // k = 2t, 2t+1 and 2t+8, 2t+9
+                y[i][0] = cmul(y[i][0], make_float2(w0.x, w0.y));
+                y[i][1] = cmul(y[i][1], make_float2(w0.z, w0.w));
+                y[i][2] = cmul(y[i][2], make_float2(w1.x, w1.y));
+                y[i][3] = cmul(y[i][3], make_float2(w1.z, w1.w));
+            }
+#pragma unroll
+            for (int j = 0; j < 4; j++) base[i][tc_pos(t, j) * Q] = y[i][j];
+        }
+    }
+}
+
+// inverse (DIT) radix-16 pass: conjugate twiddle then inverse DFT
+template <class C, int M, int TOFF, int NTH, bool SMT>
+__device__ __forceinline__ void inv_pass_tc(float2* sm, const float2* tw, int tid) {
+    constexpr int Q = M / 16, GROUPS = C::CS * (C::L / 16) / 16, NW = NTH / 32;
+    const int lane = tid & 31, g = lane >> 2, t = lane & 3;
+    TCFrag F;
+    tc_matrix(F, lane);
+    for (int grp = tid >> 5; grp < GROUPS; grp += NW) {
+        float2* base[2];
+        float2 x[2][4], y[2][4];
+#pragma unroll
+        for (int i = 0; i < 2; i++) {
+            const int it = grp * 16 + g + 8 * i;
+            const int cs = it % C::CS, b = it / C::CS, n1 = b % Q;
+            base[i] = sm + cs * C::SP + (b / Q) * M + n1;
+#pragma unroll
+            for (int j = 0; j < 4; j++) x[i][j] = base[i][tc_pos(t, j) * Q];
+            if (Q > 1) {
+                const float4* w4 = reinterpret_cast<const float4*>(tw + TOFF + n1 * 16 + 2 * t);
+                const float4 w0 = tload<SMT>(w4), w1 = tload<SMT>(w4 + 4);
+                x[i][0] = cmulc(x[i][0], make_float2(w0.x, w0.y));
+                x[i][1] = cmulc(x[i][1], make_float2(w0.z, w0.w));
+                x[i][2] = cmulc(x[i][2], make_float2(w1.x, w1.y));
+                x[i][3] = cmulc(x[i][3], make_float2(w1.z, w1.w));
+            }
+        }
+        tc_dft<true>(x, y, F);
+#pragma unroll
+        for (int i = 0; i < 2; i++)
+#pragma unroll
+            for (int j = 0; j < 4; j++) base[i][tc_pos(t, j) * Q] = y[i][j];
+    }
+}
+
+// last forward pass, derivative filter, first inverse pass (blocks of 16)
+template <class C, int NTH, bool SMT>
+__device__ __forceinline__ void mid_pass_tc(float2* sm, const float2* filt, int tid) {
+    constexpr int GROUPS = C::CS * (C::L / 16) / 16, NW = NTH / 32;
+    const int lane = tid & 31, g = lane >> 2, t = lane & 3;
+    TCFrag F;
+    tc_matrix(F, lane);
+    for (int grp = tid >> 5; grp < GROUPS; grp += NW) {
+        float2* base[2];
+        int blks[2];
+        float2 x[2][4], y[2][4];
+#pragma unroll
+        for (int i = 0; i < 2; i++) {
+            const int it = grp * 16 + g + 8 * i;
+            const int cs = it % C::CS;
+            blks[i] = it / C::CS;
+            base[i] = sm + cs * C::SP + blks[i] * 16;
+#pragma unroll
+            for (int j = 0; j < 4; j++) x[i][j] = base[i][tc_pos(t, j)];
+        }
+        tc_dft<false>(x, y, F);
+#pragma unroll
+        for (int i = 0; i < 2; i++) {
+            const float4* f4 = reinterpret_cast<const float4*>(filt + blks[i] * 16 + 2 * t);
+            const float4 f0 = tload<SMT>(f4), f1 = tload<SMT>(f4 + 4);
+            y[i][0] = cmul(y[i][0], make_float2(f0.x, f0.y));
+            y[i][1] = cmul(y[i][1], make_float2(f0.z, f0.w));
+            y[i][2] = cmul(y[i][2], make_float2(f1.x, f1.y));
+            y[i][3] = cmul(y[i][3], make_float2(f1.z, f1.w));
+        }
+        tc_dft<true>(y, x, F);
+#pragma unroll
+        for (int i = 0; i < 2; i++)
+#pragma unroll
+            for (int j = 0; j < 4; j++) base[i][tc_pos(t, j)] = x[i][j];
+    }
+}
+
 template <class C, int R, int M, int TOFF, int NTH, bool SMT>
 __device__ __forceinline__ void fwd_pass(float2* sm, const float2* tw, int tid) {
+    if constexpr (C::TC && R == 16) {
+        fwd_pass_tc<C, M, TOFF, NTH, SMT>(sm, tw, tid);
+        return;
+    }
     constexpr int Q = M / R;
     constexpr int ITEMS = C::CS * (C::L / R);
     for (int it = tid; it < ITEMS; it += NTH) {
@@ -212,6 +441,10 @@ __device__ __forceinline__ void fwd_pass(float2* sm, const float2* tw, int tid) 
 
 template <class C, int R, int M, int TOFF, int NTH, bool SMT>
 __device__ __forceinline__ void inv_pass(float2* sm, const float2* tw, int tid) {
+    if constexpr (C::TC && R == 16) {
+        inv_pass_tc<C, M, TOFF, NTH, SMT>(sm, tw, tid);
+        return;
+    }
     constexpr int Q = M / R;
     constexpr int ITEMS = C::CS * (C::L / R);
     for (int it = tid; it < ITEMS; it += NTH) {
@@ -236,6 +469,10 @@ __device__ __forceinline__ void inv_pass(float2* sm, const float2* tw, int tid) 
 // last forward pass (blocks of R contiguous positions), filter, first inverse pass
 template <class C, int R, int NTH, bool SMT>
 __device__ __forceinline__ void mid_pass(float2* sm, const float2* filt, int tid) {
+    if constexpr (C::TC && R == 16) {
+        mid_pass_tc<C, NTH, SMT>(sm, filt, tid);
+        return;
+    }
     constexpr int ITEMS = C::CS * (C::L / R);
     for (int it = tid; it < ITEMS; it += NTH) {
         const int cs = it % C::CS, blk = it / C::CS;
@@ -1151,6 +1388,7 @@ StageVariant make_pipe_variant(const char* name) {
     v.r[0] = C::R0; v.r[1] = C::R1; v.r[2] = C::R2; v.r[3] = C::R3;
     v.persistent = false;
     v.pipe = true;
+    v.bf16 = false;
     v.launch = &launch_pipe_t<C>;
     v.prepare = &prepare_pipe_t<C>;
     v.smem_for = &pipe_smem<C>;
@@ -1192,6 +1430,7 @@ StageVariant make_variant(const char* name) {
     v.r[0] = C::R0; v.r[1] = C::R1; v.r[2] = C::R2; v.r[3] = C::R3;
     v.persistent = C::NTP > 0;
     v.pipe = false;
+    v.bf16 = C::TC != 0;
     v.launch = &launch_stage_t<C>;
     v.prepare = &prepare_stage_t<C>;
     v.smem_for = &plain_smem<C>;
