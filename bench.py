@@ -54,6 +54,14 @@ def workload(name: str, seed: int):
                                                   "alpha 0.3 + 50-cell PML edges, 4 speakers, 16 receivers")
     if name == "square":
         return scenes.plain_square(seed), "square 200x200 cells + 50-cell PML, 1 speaker, 4 receivers"
+    if name == "square1200":
+        from openpstd_gb300.config import PSTDConfiguration
+        conf = PSTDConfiguration()
+        scenes.base_settings(conf, 1000, dx=0.2, pml=50)
+        conf.Domains = [scenes._domain(0, 0, 1200, 1200, 0.2, dict(left=0.0, right=0.0, top=0.0, bottom=0.0))]
+        conf.Speakers = [(120.05, 130.05, 0.0)]
+        conf.Receivers = [(200.05, 150.05, 0.0)]
+        return conf, "square 1200x1200 cells, rigid edges (transform length 2048 only), 1 speaker, 1 receiver"
     if name == "large":
         return scenes.large_square(seed, half=4096, steps=1000), (
             "8192x8192 cells as 2x2 domains of 4096x4096 with windowed interfaces, 50-cell PML (alpha 1) on the "

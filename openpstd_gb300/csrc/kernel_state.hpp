@@ -104,6 +104,24 @@ inline int fp32_variants(const StageVariant* vs, int nv) {
     return n;
 }
 
+// PSTD_PLAN="L:i,L:i,..." pins the variant of each listed strip length (for
+// profiling a plan the autotuner chose without a profiler); -1 = not listed
+inline int planned_variant(int L) {
+    const char* e = std::getenv("PSTD_PLAN");
+    if (!e) return -1;
+    std::string s(e);
+    size_t at = 0;
+    while (at < s.size()) {
+        size_t end = s.find(',', at);
+        if (end == std::string::npos) end = s.size();
+        const std::string item = s.substr(at, end - at);
+        const size_t c = item.find(':');
+        if (c != std::string::npos && std::atoi(item.substr(0, c).c_str()) == L) return std::atoi(item.c_str() + c + 1);
+        at = end + 1;
+    }
+    return -1;
+}
+
 struct Bucket {
     int L = 0;
     const StageVariant* var = nullptr;
@@ -111,6 +129,7 @@ struct Bucket {
     int tw_off = 0;                // float2 offset of the twiddles in dtw
     int fp_off = 0, fv_off = 0;    // float2 offsets of the pressure / velocity filters
     int rc = 4;                    // floats staged per strip by the pipelined form
+    bool pinned = false;           // variant fixed by PSTD_PLAN / PSTD_DFT: not tuned
     std::string choice;            // autotune record
 };
 
@@ -451,7 +470,12 @@ struct Kernel {
             if (b.var->smem_for(b.rc) > (size_t)smem_optin) b.var = &vs[0];   // pinned form does not fit
             if (want_bf16_dft())
                 for (int i = 0; i < nv; i++)
-                    if (vs[i].bf16) { b.var = &vs[i]; b.choice = " split-BF16 DFT (precision study)"; }
+                    if (vs[i].bf16) { b.var = &vs[i]; b.choice = " split-BF16 DFT (precision study)"; b.pinned = true; }
+            if (int i = planned_variant(L); i >= 0 && i < nv_fp32) {
+                b.var = &vs[i];
+                b.choice = " pinned by PSTD_PLAN";
+                b.pinned = true;
+            }
             if (forced >= 0) b.choice = " pinned";
             buckets.push_back(b);
         }
@@ -566,7 +590,7 @@ struct Kernel {
             for (size_t bi = 0; bi < buckets.size(); bi++) {
                 auto& b = buckets[bi];
                 if (tune_only && !(*tune_only)[bi]) continue;
-                if (b.var->bf16) continue;   // the precision-study form is chosen, not tuned
+                if (b.pinned) continue;   // chosen by PSTD_PLAN or the precision study, not tuned
                 const StageVariant* vs;
                 int nv = stage_variants(b.L, &vs);
                 if (nv <= 1) continue;
