@@ -9,16 +9,18 @@ const StageVariant* stage_variants_huge(int L, int* n) {
         make_variant<Cfg<4096, 4, 512, 1, 16, 16, 16>>("L4096 cs4 nt512 r16.16.16"),
         make_variant<Cfg<4096, 1, 256, 1, 16, 16, 16, 0, 128>>("L4096 cs1 ws256+128 r16.16.16"),
         make_pipe_variant<Cfg<4096, 1, 256, 1, 16, 16, 16>>("L4096 cs1 pipe256 r16.16.16"),
+        make_variant<Cfg<4096, 2, 512, 2, 16, 16, 16>>("L4096 cs2 nt512 mb2 r16.16.16"),
         make_variant<Cfg<4096, 1, 256, 2, 16, 16, 16, 0, 0, 1>>("L4096 cs1 nt256 r16.16.16 bf16x3"),
     };
     static const StageVariant v8192[] = {
         make_variant<Cfg<8192, 1, 256, 3, 16, 16, 8, 4>>("L8192 cs1 nt256 r16.16.8.4"),
         make_variant<Cfg<8192, 2, 512, 1, 16, 16, 8, 4>>("L8192 cs2 nt512 r16.16.8.4"),
+        make_variant<Cfg<8192, 1, 512, 2, 16, 16, 8, 4>>("L8192 cs1 nt512 mb2 r16.16.8.4"),
         make_variant<Cfg<8192, 1, 256, 2, 16, 16, 16, 2, 0, 1>>("L8192 cs1 nt256 r16.16.16.2 bf16x3"),
     };
     switch (L) {
-        case 4096: *n = 5; return v4096;
-        case 8192: *n = 3; return v8192;
+        case 4096: *n = 6; return v4096;
+        case 8192: *n = 4; return v8192;
         default: *n = 0; return nullptr;
     }
 }

@@ -412,8 +412,10 @@ __device__ __forceinline__ void mid_pass_tc(float2* sm, const float2* filt, int 
     }
 }
 
-template <class C, int R, int M, int TOFF, int NTH, bool SMT>
-__device__ __forceinline__ void fwd_pass(float2* sm, const float2* tw, int tid) {
+// PRUNE (first pass, M = L): positions at or past `lim` hold the zero padding
+// and are not loaded (nor stored by the gather)
+template <class C, int R, int M, int TOFF, int NTH, bool SMT, bool PRUNE = false>
+__device__ __forceinline__ void fwd_pass(float2* sm, const float2* tw, int tid, int lim = 0) {
     if constexpr (C::TC && R == 16) {
         fwd_pass_tc<C, M, TOFF, NTH, SMT>(sm, tw, tid);
         return;
@@ -428,7 +430,8 @@ __device__ __forceinline__ void fwd_pass(float2* sm, const float2* tw, int tid) 
         float2* base = sm + cs * C::SP + blk * M + n1;
         float2 x[R];
 #pragma unroll
-        for (int q = 0; q < R; q++) x[q] = base[q * Q];
+        for (int q = 0; q < R; q++)
+            x[q] = (!PRUNE || n1 + q * Q < lim) ? base[q * Q] : make_float2(0.f, 0.f);
         DFT<R, false>::run(x);
         if (Q > 1) {
 #pragma unroll
@@ -439,8 +442,10 @@ __device__ __forceinline__ void fwd_pass(float2* sm, const float2* tw, int tid) 
     }
 }
 
-template <class C, int R, int M, int TOFF, int NTH, bool SMT>
-__device__ __forceinline__ void inv_pass(float2* sm, const float2* tw, int tid) {
+// PRUNE (last pass, M = L): only positions in [lo, hi) -- the ones the
+// epilogue reads -- are stored
+template <class C, int R, int M, int TOFF, int NTH, bool SMT, bool PRUNE = false>
+__device__ __forceinline__ void inv_pass(float2* sm, const float2* tw, int tid, int lo = 0, int hi = 0) {
     if constexpr (C::TC && R == 16) {
         inv_pass_tc<C, M, TOFF, NTH, SMT>(sm, tw, tid);
         return;
@@ -462,7 +467,8 @@ __device__ __forceinline__ void inv_pass(float2* sm, const float2* tw, int tid) 
         }
         DFT<R, true>::run(x);
 #pragma unroll
-        for (int q = 0; q < R; q++) base[q * Q] = x[q];
+        for (int q = 0; q < R; q++)
+            if (!PRUNE || (n1 + q * Q >= lo && n1 + q * Q < hi)) base[q * Q] = x[q];
     }
 }
 
@@ -495,18 +501,21 @@ __device__ __forceinline__ void mid_pass(float2* sm, const float2* filt, int tid
     }
 }
 
-template <class C, int NTH, int BAR, bool SMT>
-__device__ __forceinline__ void convolve(float2* sm, const float2* tw, const float2* filt, int tid) {
+// PRUNE: the input is zero at and past z0 (not materialised) and only the
+// output positions [lo, hi) are needed
+template <class C, int NTH, int BAR, bool SMT, bool PRUNE = false>
+__device__ __forceinline__ void convolve(float2* sm, const float2* tw, const float2* filt, int tid, int z0 = 0,
+                                         int lo = 0, int hi = 0) {
     constexpr int M0 = C::L, M1 = C::M1, M2 = C::M2;
     constexpr int T0 = 0, T1 = M0, T2 = M0 + M1;
     if constexpr (C::NP == 2) {
-        fwd_pass<C, C::R0, M0, T0, NTH, SMT>(sm, tw, tid);
+        fwd_pass<C, C::R0, M0, T0, NTH, SMT, PRUNE>(sm, tw, tid, z0);
         group_sync<BAR, NTH>();
         mid_pass<C, C::R1, NTH, SMT>(sm, filt, tid);
         group_sync<BAR, NTH>();
-        inv_pass<C, C::R0, M0, T0, NTH, SMT>(sm, tw, tid);
+        inv_pass<C, C::R0, M0, T0, NTH, SMT, PRUNE>(sm, tw, tid, lo, hi);
     } else if constexpr (C::NP == 3) {
-        fwd_pass<C, C::R0, M0, T0, NTH, SMT>(sm, tw, tid);
+        fwd_pass<C, C::R0, M0, T0, NTH, SMT, PRUNE>(sm, tw, tid, z0);
         group_sync<BAR, NTH>();
         fwd_pass<C, C::R1, M1, T1, NTH, SMT>(sm, tw, tid);
         group_sync<BAR, NTH>();
@@ -514,9 +523,9 @@ __device__ __forceinline__ void convolve(float2* sm, const float2* tw, const flo
         group_sync<BAR, NTH>();
         inv_pass<C, C::R1, M1, T1, NTH, SMT>(sm, tw, tid);
         group_sync<BAR, NTH>();
-        inv_pass<C, C::R0, M0, T0, NTH, SMT>(sm, tw, tid);
+        inv_pass<C, C::R0, M0, T0, NTH, SMT, PRUNE>(sm, tw, tid, lo, hi);
     } else {
-        fwd_pass<C, C::R0, M0, T0, NTH, SMT>(sm, tw, tid);
+        fwd_pass<C, C::R0, M0, T0, NTH, SMT, PRUNE>(sm, tw, tid, z0);
         group_sync<BAR, NTH>();
         fwd_pass<C, C::R1, M1, T1, NTH, SMT>(sm, tw, tid);
         group_sync<BAR, NTH>();
@@ -528,7 +537,7 @@ __device__ __forceinline__ void convolve(float2* sm, const float2* tw, const flo
         group_sync<BAR, NTH>();
         inv_pass<C, C::R1, M1, T1, NTH, SMT>(sm, tw, tid);
         group_sync<BAR, NTH>();
-        inv_pass<C, C::R0, M0, T0, NTH, SMT>(sm, tw, tid);
+        inv_pass<C, C::R0, M0, T0, NTH, SMT, PRUNE>(sm, tw, tid, lo, hi);
     }
 }
 
@@ -632,7 +641,7 @@ __device__ void copy_axis(const StageArgs& A, const DevDomain& D, bool ydir, int
 }
 
 // ---- step 1: strips + bands + padding of one job into `sm` (NTH threads)
-template <class C, int NTH>
+template <class C, int NTH, bool ZERO = true>
 __device__ __forceinline__ void gather(float2* sm, const StageArgs& A, const DevJob& job, const DevDomain& dom,
                                        bool first, int tid) {
     constexpr int CS = C::CS, SP = C::SP, L = C::L, S2 = 2 * CS;
@@ -782,10 +791,13 @@ __device__ __forceinline__ void gather(float2* sm, const StageArgs& A, const Dev
             smf[2 * ((s >> 1) * SP + pos) + (s & 1)] = val;
         }
     }
-    // zero padding [2W+n, L) of every complex strip
-    const int z0 = 2 * W + n;
-    for (int cs = warp; cs < CS; cs += NW)
-        for (int p = z0 + lane; p < L; p += 32) sm[cs * SP + p] = make_float2(0.f, 0.f);
+    // zero padding [2W+n, L) of every complex strip (a pruned first pass does
+    // not read it)
+    if constexpr (ZERO) {
+        const int z0 = 2 * W + n;
+        for (int cs = warp; cs < CS; cs += NW)
+            for (int p = z0 + lane; p < L; p += 32) sm[cs * SP + p] = make_float2(0.f, 0.f);
+    }
 }
 
 // ---- L2 prefetch of everything a job streams: the strip rows / columns of
@@ -983,9 +995,14 @@ __global__ void __launch_bounds__(C::NT, C::MINB) stage_kernel(StageArgs A) {
     }
     const bool first = A.first_step[dom.scene] != 0;
     prefetch_job<C, C::NT>(A, job, dom, first, threadIdx.x);
-    gather<C, C::NT>(sm, A, job, dom, first, threadIdx.x);
+    constexpr bool PRUNE = !C::TC;   // the tensor-core passes read the padding
+    gather<C, C::NT, !PRUNE>(sm, A, job, dom, first, threadIdx.x);
     __syncthreads();
-    convolve<C, C::NT, 0, false>(sm, A.tw, A.filt + job.dtab, threadIdx.x);
+    const bool vel = job.kind & JK_VEL;
+    const int n = ((job.kind & JK_Y) ? dom.ny : dom.nx) + (vel ? 1 : 0);
+    const int nout = vel ? n - 1 : n + 1;
+    convolve<C, C::NT, 0, false, PRUNE>(sm, A.tw, A.filt + job.dtab, threadIdx.x, 2 * job.W + n, job.W,
+                                         job.W + nout);
     __syncthreads();
     epilogue<C, C::NT>(sm, A, job, dom, threadIdx.x);
 }

@@ -12,9 +12,11 @@ const StageVariant* stage_variants_large(int L, int* n) {
         make_variant<Cfg<2048, 4, 256, 1, 16, 16, 8, 0, 384>>("L2048 cs4 ws256+384 r16.16.8"),
         make_pipe_variant<Cfg<2048, 2, 256, 1, 16, 16, 8>>("L2048 cs2 pipe256 r16.16.8"),
         make_pipe_variant<Cfg<2048, 1, 128, 2, 16, 16, 8>>("L2048 cs1 pipe128 r16.16.8"),
+        make_variant<Cfg<2048, 4, 512, 2, 16, 16, 8>>("L2048 cs4 nt512 mb2 r16.16.8"),
+        make_variant<Cfg<2048, 2, 256, 4, 16, 16, 8>>("L2048 cs2 nt256 mb4 r16.16.8"),
     };
     switch (L) {
-        case 2048: *n = 7; return v2048;
+        case 2048: *n = 9; return v2048;
         default: *n = 0; return nullptr;
     }
 }
