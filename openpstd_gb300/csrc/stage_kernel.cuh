@@ -850,14 +850,24 @@ __device__ __forceinline__ void prefetch_job(const StageArgs& A, const DevJob& j
 // ---- step 5: slice, RK update, (sixth stage) PML on vx / vy
 // RK update of one value in the reference's operation order
 // (kernel/Solver.cpp:174-181): v0 - (dt*a_k) * (L / rho) and p0 - (dt*a_k) * ((L*rho)*c^2)
-__device__ __forceinline__ float rk_update(float prev, float d, bool vel, float cdt, float rho, float c2) {
-    return vel ? __fsub_rn(prev, __fmul_rn(cdt, __fmul_rn(__fmul_rn(d, rho), c2)))
-               : __fsub_rn(prev, __fmul_rn(cdt, __fdiv_rn(d, rho)));
+__device__ __forceinline__ float div_rho(float d, float rho, float rinv) {
+    // d / rho correctly rounded from the correctly rounded reciprocal rinv:
+    // q = d * rinv, exact residual r = d - q * rho (FMA), q + r * rinv
+    // (Markstein's division correction, "IA-64 and Elementary Functions",
+    // 2000, section 8); rho is a finite normal density, d a field derivative
+    const float q = __fmul_rn(d, rinv);
+    const float r = __fmaf_rn(-q, rho, d);
+    return __fmaf_rn(r, rinv, q);
 }
 
-template <class C, int NTH>
-__device__ __forceinline__ void epilogue(const float2* sm, const StageArgs& A, const DevJob& job, const DevDomain& dom,
-                                         int tid) {
+__device__ __forceinline__ float rk_update(float prev, float d, bool vel, float cdt, float rho, float c2, float rinv) {
+    return vel ? __fsub_rn(prev, __fmul_rn(cdt, __fmul_rn(__fmul_rn(d, rho), c2)))
+               : __fsub_rn(prev, __fmul_rn(cdt, div_rho(d, rho, rinv)));
+}
+
+template <class C, int NTH, bool VEL>
+__device__ __forceinline__ void epilogue_k(const float2* sm, const StageArgs& A, const DevJob& job, const DevDomain& dom,
+                                           int tid) {
     constexpr int CS = C::CS, SP = C::SP, S2 = 2 * CS;
     constexpr int NW = NTH / 32;
     constexpr int WPP = NW >= CS ? NW / CS : 1;
@@ -866,7 +876,7 @@ __device__ __forceinline__ void epilogue(const float2* sm, const StageArgs& A, c
     const float* __restrict__ prev = A.prev;
     float* __restrict__ out = A.out;
     const int warp = tid >> 5, lane = tid & 31;
-    const bool vel = job.kind & JK_VEL;
+    constexpr bool vel = VEL;
     const bool ydir = job.kind & JK_Y;
     const int W = job.W;
     const int n = (ydir ? dom.ny : dom.nx) + (vel ? 1 : 0);
@@ -874,6 +884,7 @@ __device__ __forceinline__ void epilogue(const float2* sm, const StageArgs& A, c
     const float cdt = A.doms[job.dom].cdt[A.stage];
     const float rho = dom.rho;
     const float c2 = dom.c2;
+    const float rinv = __frcp_rn(rho);
     const int nout = vel ? n - 1 : n + 1;   // cells (vel) or faces (pressure)
     long long fo;
     int fp, ao;
@@ -912,7 +923,7 @@ __device__ __forceinline__ void epilogue(const float2* sm, const StageArgs& A, c
                         float v[4] = {p[q][h].x, p[q][h].y, p[q][h].z, p[q][h].w};
 #pragma unroll
                         for (int e = 0; e < 4; e++) {
-                            v[e] = rk_update(v[e], h ? d[e].y : d[e].x, vel, cdt, rho, c2);
+                            v[e] = rk_update(v[e], h ? d[e].y : d[e].x, vel, cdt, rho, c2, rinv);
                             if (att && i + e < nout) v[e] = __fmul_rn(v[e], A.att[ao + i + e]);
                         }
                         float* o = out + r0 + (h ? fp : 0) + i;
@@ -947,8 +958,8 @@ __device__ __forceinline__ void epilogue(const float2* sm, const StageArgs& A, c
                 if (f >= total) continue;
                 const int g = f % G, i = f / G;
                 const float2 d0 = sm[2 * g * SP + W + i], d1 = sm[(2 * g + 1) * SP + W + i];
-                float v[4] = {rk_update(pv[q].x, d0.x, vel, cdt, rho, c2), rk_update(pv[q].y, d0.y, vel, cdt, rho, c2),
-                              rk_update(pv[q].z, d1.x, vel, cdt, rho, c2), rk_update(pv[q].w, d1.y, vel, cdt, rho, c2)};
+                float v[4] = {rk_update(pv[q].x, d0.x, vel, cdt, rho, c2, rinv), rk_update(pv[q].y, d0.y, vel, cdt, rho, c2, rinv),
+                              rk_update(pv[q].z, d1.x, vel, cdt, rho, c2, rinv), rk_update(pv[q].w, d1.y, vel, cdt, rho, c2, rinv)};
                 if (att) {
                     const float a = A.att[ao + i];
 #pragma unroll
@@ -975,12 +986,21 @@ __device__ __forceinline__ void epilogue(const float2* sm, const StageArgs& A, c
                 const int s = f % S2, i = f / S2;
                 if (f >= total || s >= count) continue;
                 const float dv = smf[2 * ((s >> 1) * SP + W + i) + (s & 1)];
-                float v = rk_update(pv[q], dv, vel, cdt, rho, c2);
+                float v = rk_update(pv[q], dv, vel, cdt, rho, c2, rinv);
                 if (att) v = __fmul_rn(v, A.att[ao + i]);
                 out[fo + (long long)i * fp + job.first + s] = v;
             }
         }
     }
+}
+
+// the update arithmetic differs between velocity and pressure derivatives:
+// one instantiation each, chosen once per job
+template <class C, int NTH>
+__device__ __forceinline__ void epilogue(const float2* sm, const StageArgs& A, const DevJob& job, const DevDomain& dom,
+                                         int tid) {
+    if (job.kind & JK_VEL) epilogue_k<C, NTH, true>(sm, A, job, dom, tid);
+    else epilogue_k<C, NTH, false>(sm, A, job, dom, tid);
 }
 
 // ---------------------------------------------------------------- plain form
@@ -1267,7 +1287,7 @@ __device__ __forceinline__ void pipe_epilogue(const float2* sm, const float* slo
     const float* sp = slot + 2 * S2 * rc;
     float* __restrict__ out = A.out;
     const float cdt = A.doms[job.dom].cdt[A.stage];
-    const float rho = dom.rho, c2 = dom.c2;
+    const float rho = dom.rho, c2 = dom.c2, rinv = __frcp_rn(rho);
     const int W = g.W, nout = g.nout;
     const bool att = A.last && g.ao >= 0;
     if (!g.ydir) {
@@ -1279,7 +1299,7 @@ __device__ __forceinline__ void pipe_epilogue(const float2* sm, const float* slo
             float v[4] = {pv.x, pv.y, pv.z, pv.w};
 #pragma unroll
             for (int e = 0; e < 4; e++) {
-                v[e] = rk_update(v[e], dv[2 * e], g.vel, cdt, rho, c2);
+                v[e] = rk_update(v[e], dv[2 * e], g.vel, cdt, rho, c2, rinv);
                 if (att && i + e < nout) v[e] = __fmul_rn(v[e], A.att[g.ao + i + e]);
             }
             float* o = out + g.fo + (long long)(job.first + s) * g.fp + i;
@@ -1297,8 +1317,8 @@ __device__ __forceinline__ void pipe_epilogue(const float2* sm, const float* slo
             const int q = k % G, i = k / G;
             const float4 pv = *reinterpret_cast<const float4*>(sp + i * S2 + 4 * q);
             const float2 d0 = sm[2 * q * SP + W + i], d1 = sm[(2 * q + 1) * SP + W + i];
-            float v[4] = {rk_update(pv.x, d0.x, g.vel, cdt, rho, c2), rk_update(pv.y, d0.y, g.vel, cdt, rho, c2),
-                          rk_update(pv.z, d1.x, g.vel, cdt, rho, c2), rk_update(pv.w, d1.y, g.vel, cdt, rho, c2)};
+            float v[4] = {rk_update(pv.x, d0.x, g.vel, cdt, rho, c2, rinv), rk_update(pv.y, d0.y, g.vel, cdt, rho, c2, rinv),
+                          rk_update(pv.z, d1.x, g.vel, cdt, rho, c2, rinv), rk_update(pv.w, d1.y, g.vel, cdt, rho, c2, rinv)};
             if (att) {
                 const float a = A.att[g.ao + i];
 #pragma unroll
@@ -1311,7 +1331,7 @@ __device__ __forceinline__ void pipe_epilogue(const float2* sm, const float* slo
         const float* smf = reinterpret_cast<const float*>(sm);
         for (int k = tid; k < g.count * nout; k += NTH) {
             const int s = k % g.count, i = k / g.count;
-            float v = rk_update(sp[i * S2 + s], smf[2 * ((s >> 1) * SP + W + i) + (s & 1)], g.vel, cdt, rho, c2);
+            float v = rk_update(sp[i * S2 + s], smf[2 * ((s >> 1) * SP + W + i) + (s & 1)], g.vel, cdt, rho, c2, rinv);
             if (att) v = __fmul_rn(v, A.att[g.ao + i]);
             out[g.fo + (long long)i * g.fp + job.first + s] = v;
         }
