@@ -641,9 +641,10 @@ __device__ void copy_axis(const StageArgs& A, const DevDomain& D, bool ydir, int
 }
 
 // ---- step 1: strips + bands + padding of one job into `sm` (NTH threads)
-template <class C, int NTH, bool ZERO = true>
-__device__ __forceinline__ void gather(float2* sm, const StageArgs& A, const DevJob& job, const DevDomain& dom,
-                                       bool first, int tid) {
+// TWO: the strip's p0 is formed as px + py (else one field: velocity or stale p0)
+template <class C, int NTH, bool ZERO, bool TWO>
+__device__ __forceinline__ void gather_k(float2* sm, const StageArgs& A, const DevJob& job, const DevDomain& dom,
+                                         bool first, const Src& S, int tid) {
     constexpr int CS = C::CS, SP = C::SP, L = C::L, S2 = 2 * CS;
     constexpr int NW = NTH / 32;
     constexpr int WPP = NW >= CS ? NW / CS : 1;   // warps per strip pair
@@ -655,14 +656,13 @@ __device__ __forceinline__ void gather(float2* sm, const StageArgs& A, const Dev
     const int W = job.W;
     const int n = (ydir ? dom.ny : dom.nx) + (vel ? 1 : 0);
     const int count = job.count;
-    const Src S = strip_source(A, dom, vel, ydir, first);
     if (!ydir) {
         // row pairs (2cs, 2cs+1), 16-byte loads, four chunks per lane in flight
         const int chunks = (n + 3) >> 2;
         for (int cs = warp / WPP; cs < CS; cs += PST) {
             const int s0 = 2 * cs;
             const float* a0 = S.a + (long long)(job.first + s0) * S.pitch;
-            const float* b0 = S.b ? S.b + (long long)(job.first + s0) * S.pitch : nullptr;
+            const float* b0 = TWO ? S.b + (long long)(job.first + s0) * S.pitch : nullptr;
             const bool h0 = s0 < count, h1 = s0 + 1 < count;
             for (int c0 = (warp % WPP) * 32 + lane; c0 < chunks; c0 += 4 * WPP * 32) {
                 float4 u[4], v[4];
@@ -671,8 +671,9 @@ __device__ __forceinline__ void gather(float2* sm, const StageArgs& A, const Dev
                     const int c = c0 + q * WPP * 32, i = c << 2;
                     u[q] = v[q] = make_float4(0.f, 0.f, 0.f, 0.f);
                     if (c < chunks) {
-                        if (h0) u[q] = b0 ? add4(ld4(a0, i, n), ld4(b0, i, n)) : ld4(a0, i, n);
-                        if (h1) v[q] = b0 ? add4(ld4(a0 + S.pitch, i, n), ld4(b0 + S.pitch, i, n)) : ld4(a0 + S.pitch, i, n);
+                        // whole 16-byte quads: every row is padded past its last quad
+                        if (h0) u[q] = TWO ? add4(ldf4(a0 + i), ldf4(b0 + i)) : ldf4(a0 + i);
+                        if (h1) v[q] = TWO ? add4(ldf4(a0 + S.pitch + i), ldf4(b0 + S.pitch + i)) : ldf4(a0 + S.pitch + i);
                     }
                 }
 #pragma unroll
@@ -702,7 +703,7 @@ __device__ __forceinline__ void gather(float2* sm, const StageArgs& A, const Dev
                 if (f < total) {
                     const int g = f % G, i = f / G;
                     const float* a = S.a + (long long)i * S.pitch + job.first + 4 * g;
-                    u[q] = S.b ? add4(ldf4(a), ldf4(S.b + (a - S.a))) : ldf4(a);
+                    u[q] = TWO ? add4(ldf4(a), ldf4(S.b + (a - S.a))) : ldf4(a);
                 }
             }
 #pragma unroll
@@ -727,7 +728,10 @@ __device__ __forceinline__ void gather(float2* sm, const StageArgs& A, const Dev
                 val[q] = 0.f;
                 if (f < total) {
                     const int s = f % S2, i = f / S2;
-                    if (s < count) val[q] = S.at((long long)i * S.pitch + job.first + s);
+                    if (s < count) {
+                        const long long el = (long long)i * S.pitch + job.first + s;
+                        val[q] = TWO ? __fadd_rn(ldf(S.a + el), ldf(S.b + el)) : ldf(S.a + el);
+                    }
                 }
             }
 #pragma unroll
@@ -800,6 +804,14 @@ __device__ __forceinline__ void gather(float2* sm, const StageArgs& A, const Dev
     }
 }
 
+template <class C, int NTH, bool ZERO = true>
+__device__ __forceinline__ void gather(float2* sm, const StageArgs& A, const DevJob& job, const DevDomain& dom,
+                                       bool first, int tid) {
+    const Src S = strip_source(A, dom, job.kind & JK_VEL, job.kind & JK_Y, first);
+    if (S.b) gather_k<C, NTH, ZERO, true>(sm, A, job, dom, first, S, tid);
+    else gather_k<C, NTH, ZERO, false>(sm, A, job, dom, first, S, tid);
+}
+
 // ---- L2 prefetch of everything a job streams: the strip rows / columns of
 // the gather and the stage-start values the epilogue reads (128-byte lines;
 // rows start on line boundaries, so every line touched lies inside its row)
@@ -865,7 +877,7 @@ __device__ __forceinline__ float rk_update(float prev, float d, bool vel, float 
                : __fsub_rn(prev, __fmul_rn(cdt, div_rho(d, rho, rinv)));
 }
 
-template <class C, int NTH, bool VEL>
+template <class C, int NTH, bool VEL, bool ATT>
 __device__ __forceinline__ void epilogue_k(const float2* sm, const StageArgs& A, const DevJob& job, const DevDomain& dom,
                                            int tid) {
     constexpr int CS = C::CS, SP = C::SP, S2 = 2 * CS;
@@ -890,7 +902,7 @@ __device__ __forceinline__ void epilogue_k(const float2* sm, const StageArgs& A,
     int fp, ao;
     if (!vel) { fo = ydir ? dom.o_vy : dom.o_vx; fp = ydir ? dom.pitch_vy : dom.pitch_vx; ao = ydir ? dom.att_yv : dom.att_xv; }
     else { fo = ydir ? dom.o_py : dom.o_px; fp = dom.pitch_p; ao = -1; }
-    const bool att = A.last && ao >= 0;
+    constexpr bool att = ATT;   // PML multiply of vx / vy at the sixth stage
     if (!ydir) {
         // rows: four consecutive outputs per lane (16-byte loads / stores), two chunks in flight
         const int chunks = (nout + 3) >> 2;
@@ -906,8 +918,9 @@ __device__ __forceinline__ void epilogue_k(const float2* sm, const StageArgs& A,
                     const int i = (c0 + q * WPP * 32) << 2;
                     p[q][0] = p[q][1] = make_float4(0.f, 0.f, 0.f, 0.f);
                     if (i < nout) {
-                        p[q][0] = ld4(prev + r0, i, nout);
-                        if (h1) p[q][1] = ld4(prev + r0 + fp, i, nout);
+                        // whole quads: rows are padded past their last quad
+                        p[q][0] = ldf4(prev + r0 + i);
+                        if (h1) p[q][1] = ldf4(prev + r0 + fp + i);
                     }
                 }
 #pragma unroll
@@ -999,8 +1012,10 @@ __device__ __forceinline__ void epilogue_k(const float2* sm, const StageArgs& A,
 template <class C, int NTH>
 __device__ __forceinline__ void epilogue(const float2* sm, const StageArgs& A, const DevJob& job, const DevDomain& dom,
                                          int tid) {
-    if (job.kind & JK_VEL) epilogue_k<C, NTH, true>(sm, A, job, dom, tid);
-    else epilogue_k<C, NTH, false>(sm, A, job, dom, tid);
+    const int ao = (job.kind & JK_Y) ? dom.att_yv : dom.att_xv;
+    if (job.kind & JK_VEL) epilogue_k<C, NTH, true, false>(sm, A, job, dom, tid);
+    else if (A.last && ao >= 0) epilogue_k<C, NTH, false, true>(sm, A, job, dom, tid);
+    else epilogue_k<C, NTH, false, false>(sm, A, job, dom, tid);
 }
 
 // ---------------------------------------------------------------- plain form
