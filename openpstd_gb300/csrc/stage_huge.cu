@@ -16,11 +16,12 @@ const StageVariant* stage_variants_huge(int L, int* n) {
         make_variant<Cfg<8192, 1, 256, 3, 16, 16, 8, 4>>("L8192 cs1 nt256 r16.16.8.4"),
         make_variant<Cfg<8192, 2, 512, 1, 16, 16, 8, 4>>("L8192 cs2 nt512 r16.16.8.4"),
         make_variant<Cfg<8192, 1, 512, 2, 16, 16, 8, 4>>("L8192 cs1 nt512 mb2 r16.16.8.4"),
+        make_variant<Cfg<8192, 1, 256, 2, 32, 16, 16>>("L8192 cs1 nt256 mb2 r32.16.16"),
         make_variant<Cfg<8192, 1, 256, 2, 16, 16, 16, 2, 0, 1>>("L8192 cs1 nt256 r16.16.16.2 bf16x3"),
     };
     switch (L) {
         case 4096: *n = 6; return v4096;
-        case 8192: *n = 4; return v8192;
+        case 8192: *n = 5; return v8192;
         default: *n = 0; return nullptr;
     }
 }

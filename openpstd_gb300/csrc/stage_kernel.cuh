@@ -141,6 +141,50 @@ struct DFT<16, INV> {
     }
 };
 
+// a * exp(-/+ 2 pi i K / 32); odd K use cos / sin of multiples of pi/16
+#define PSTD_C16 0.98078528040323044913f   // cos(pi/16)
+#define PSTD_S16 0.19509032201612826785f   // sin(pi/16)
+#define PSTD_C316 0.83146961230254523708f  // cos(3 pi/16)
+#define PSTD_S316 0.55557023301960222474f  // sin(3 pi/16)
+template <int K, bool INV>
+__device__ __forceinline__ float2 tw32(float2 a) {
+    constexpr float sg = INV ? 1.f : -1.f;
+    if constexpr ((K & 1) == 0) {
+        return tw16<K / 2, INV>(a);
+    } else {
+        constexpr float c = K == 1 ? PSTD_C16 : K == 3 ? PSTD_C316 : K == 5 ? PSTD_S316 : K == 7 ? PSTD_S16
+                          : K == 9 ? -PSTD_S16 : K == 11 ? -PSTD_S316 : K == 13 ? -PSTD_C316 : -PSTD_C16;
+        constexpr float s = K == 1 ? PSTD_S16 : K == 3 ? PSTD_S316 : K == 5 ? PSTD_C316 : K == 7 ? PSTD_C16
+                          : K == 9 ? PSTD_C16 : K == 11 ? PSTD_C316 : K == 13 ? PSTD_S316 : PSTD_S16;
+        return cmul(a, make_float2(c, sg * s));
+    }
+}
+
+template <int K, bool INV>
+__device__ __forceinline__ void tw32_all(float2* o) {
+    if constexpr (K < 16) {
+        o[K] = tw32<K, INV>(o[K]);
+        tw32_all<K + 1, INV>(o);
+    }
+}
+
+template <bool INV>
+struct DFT<32, INV> {
+    static __device__ __forceinline__ void run(float2* x) {
+        float2 e[16], o[16];
+#pragma unroll
+        for (int k = 0; k < 16; k++) { e[k] = x[2 * k]; o[k] = x[2 * k + 1]; }
+        DFT<16, INV>::run(e);
+        DFT<16, INV>::run(o);
+        tw32_all<1, INV>(o);
+#pragma unroll
+        for (int k = 0; k < 16; k++) {
+            x[k] = cadd(e[k], o[k]);
+            x[k + 16] = csub(e[k], o[k]);
+        }
+    }
+};
+
 // ---------------------------------------------------------------- variants
 // Plain form: L, complex strips per CTA, threads, min CTAs per SM, radices.
 // Persistent form (NTP > 0): NT FFT threads + NTP memory threads.
@@ -425,17 +469,34 @@ __device__ __forceinline__ void fwd_pass(float2* sm, const float2* tw, int tid, 
     for (int it = tid; it < ITEMS; it += NTH) {
         const int cs = it % C::CS, b = it / C::CS;
         const int blk = b / Q, n1 = b % Q;
-        float2 w[R];
-        if (Q > 1) load_twiddles<R, SMT>(tw + TOFF + n1 * R, w);
         float2* base = sm + cs * C::SP + blk * M + n1;
         float2 x[R];
+        if constexpr (R == 32) {
+            // 32 values per thread: twiddles loaded pairwise after the butterfly
 #pragma unroll
-        for (int q = 0; q < R; q++)
-            x[q] = (!PRUNE || n1 + q * Q < lim) ? base[q * Q] : make_float2(0.f, 0.f);
-        DFT<R, false>::run(x);
-        if (Q > 1) {
+            for (int q = 0; q < R; q++)
+                x[q] = (!PRUNE || n1 + q * Q < lim) ? base[q * Q] : make_float2(0.f, 0.f);
+            DFT<R, false>::run(x);
+            if (Q > 1) {
+                const float4* t4 = reinterpret_cast<const float4*>(tw + TOFF + n1 * R);
 #pragma unroll
-            for (int k = 1; k < R; k++) x[k] = cmul(x[k], w[k]);
+                for (int h = 0; h < R / 2; h++) {
+                    const float4 v = tload<SMT>(t4 + h);
+                    if (h) x[2 * h] = cmul(x[2 * h], make_float2(v.x, v.y));
+                    x[2 * h + 1] = cmul(x[2 * h + 1], make_float2(v.z, v.w));
+                }
+            }
+        } else {
+            float2 w[R];
+            if (Q > 1) load_twiddles<R, SMT>(tw + TOFF + n1 * R, w);
+#pragma unroll
+            for (int q = 0; q < R; q++)
+                x[q] = (!PRUNE || n1 + q * Q < lim) ? base[q * Q] : make_float2(0.f, 0.f);
+            DFT<R, false>::run(x);
+            if (Q > 1) {
+#pragma unroll
+                for (int k = 1; k < R; k++) x[k] = cmul(x[k], w[k]);
+            }
         }
 #pragma unroll
         for (int k = 0; k < R; k++) base[k * Q] = x[k];
@@ -455,15 +516,25 @@ __device__ __forceinline__ void inv_pass(float2* sm, const float2* tw, int tid, 
     for (int it = tid; it < ITEMS; it += NTH) {
         const int cs = it % C::CS, b = it / C::CS;
         const int blk = b / Q, n1 = b % Q;
-        float2 w[R];
-        if (Q > 1) load_twiddles<R, SMT>(tw + TOFF + n1 * R, w);
         float2* base = sm + cs * C::SP + blk * M + n1;
         float2 x[R];
 #pragma unroll
         for (int k = 0; k < R; k++) x[k] = base[k * Q];
         if (Q > 1) {
+            if constexpr (R == 32) {
+                const float4* t4 = reinterpret_cast<const float4*>(tw + TOFF + n1 * R);
 #pragma unroll
-            for (int k = 1; k < R; k++) x[k] = cmulc(x[k], w[k]);
+                for (int h = 0; h < R / 2; h++) {
+                    const float4 v = tload<SMT>(t4 + h);
+                    if (h) x[2 * h] = cmulc(x[2 * h], make_float2(v.x, v.y));
+                    x[2 * h + 1] = cmulc(x[2 * h + 1], make_float2(v.z, v.w));
+                }
+            } else {
+                float2 w[R];
+                load_twiddles<R, SMT>(tw + TOFF + n1 * R, w);
+#pragma unroll
+                for (int k = 1; k < R; k++) x[k] = cmulc(x[k], w[k]);
+            }
         }
         DFT<R, true>::run(x);
 #pragma unroll
@@ -483,18 +554,16 @@ __device__ __forceinline__ void mid_pass(float2* sm, const float2* filt, int tid
     for (int it = tid; it < ITEMS; it += NTH) {
         const int cs = it % C::CS, blk = it / C::CS;
         float2* base = sm + cs * C::SP + blk * R;
-        float2 f[R], x[R];
-#pragma unroll
-        for (int h = 0; h < R / 2; h++) {
-            const float4 v = tload<SMT>(reinterpret_cast<const float4*>(filt + blk * R) + h);
-            f[2 * h] = make_float2(v.x, v.y);
-            f[2 * h + 1] = make_float2(v.z, v.w);
-        }
+        float2 x[R];
 #pragma unroll
         for (int q = 0; q < R; q++) x[q] = base[q];
         DFT<R, false>::run(x);
 #pragma unroll
-        for (int k = 0; k < R; k++) x[k] = cmul(x[k], f[k]);
+        for (int h = 0; h < R / 2; h++) {
+            const float4 v = tload<SMT>(reinterpret_cast<const float4*>(filt + blk * R) + h);
+            x[2 * h] = cmul(x[2 * h], make_float2(v.x, v.y));
+            x[2 * h + 1] = cmul(x[2 * h + 1], make_float2(v.z, v.w));
+        }
         DFT<R, true>::run(x);
 #pragma unroll
         for (int q = 0; q < R; q++) base[q] = x[q];

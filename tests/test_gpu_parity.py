@@ -238,7 +238,7 @@ def test_full_size_l_shape_superposition():
         assert rel(b, a) < 1e-5, f
 
 
-@pytest.mark.parametrize("variant", list(range(9)))
+@pytest.mark.parametrize("variant", list(range(11)))
 def test_every_stage_variant(oracle_mod, variant, monkeypatch):
     """Each compiled stage-kernel variant (strips per CTA, threads, radix
     plan) must reproduce the oracle: the autotuner may pick any of them."""
@@ -253,3 +253,5 @@ def test_every_stage_variant(oracle_mod, variant, monkeypatch):
     check_parity(oracle_mod, conf, 30, threads=16)
     conf = scenes.rect(5, nx=2000, ny=60, steps=20)    # 4096 (x strips), 128
     check_parity(oracle_mod, conf, 20, threads=16)
+    conf = scenes.rect(7, nx=4100, ny=40, steps=12)    # 8192 (x strips), 128
+    check_parity(oracle_mod, conf, 12, threads=16)
