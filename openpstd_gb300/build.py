@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpstd_gb300.so")
 
-SOURCES = ["scene.cpp", "stage_small.cu", "stage_mid.cu", "stage_large.cu", "stage_huge.cu", "misc.cu", "solver.cu", "server.cu",
+SOURCES = ["scene.cpp", "stage_small.cu", "stage_mid.cu", "stage_large.cu", "stage_huge.cu", "stage_all.cu", "misc.cu", "solver.cu", "server.cu",
            "gpu_pstd_kernel.cpp"]
 HEADERS = ["scene.hpp", "device.cuh", "launch.hpp", "stage_kernel.cuh", "kernel_state.hpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

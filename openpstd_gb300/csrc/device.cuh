@@ -55,6 +55,8 @@ struct DevJob {
     float R1, T1, R2, T2;   // reflection / transmission of the two bands
     int dtab;         // float2 offset of the permuted derivative filter
     int wtab;         // float offset of the 2W+1 window coefficients
+    int L;            // transform length (0 for a copy job)
+    int ttab;         // float2 offset of the twiddle tables of the job's radix plan
 };
 
 struct DevReceiver {

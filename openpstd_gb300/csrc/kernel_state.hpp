@@ -320,6 +320,8 @@ struct Kernel {
                     else     { j.R1 = rlw1;  j.T1 = tlw2; j.R2 = rrw1;  j.T2 = trw2; }
                     j.dtab = filter_of(L, vel, v, sc.s.dx);
                     j.wtab = wo;
+                    j.L = L;
+                    j.ttab = twiddles_of(v);
                     int s_ = r.first, end = r.first + r.count;
                     int origin = d.lo(r.axis);
                     while (s_ < end) {
@@ -531,7 +533,7 @@ struct Kernel {
         dframe_off.upload(frame_off);
         dframe.alloc(std::max<size_t>(frame_floats, 1));
 
-        // ---- tables and the job plan (autotuned)
+        // ---- tables and the job plan (autotuned), then the launch form
         reset();
         plan(autotune);
         reset();
@@ -540,7 +542,8 @@ struct Kernel {
             CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
             side.push_back(s);
         }
-        capture_graphs();
+        choose_form(autotune);
+        if (!merged) capture_graphs();
         std::string choice;
         for (auto& b : buckets) choice += " [" + std::string(b.var->name) + b.choice + "]";
         log(PSTD_LOG_DEBUG, std::to_string(scenes.size()) + " scene(s), " + std::to_string(gdom.size()) + " domains, " +
@@ -679,7 +682,132 @@ struct Kernel {
         steps = 0;
     }
 
-    int launches_per_step() const { return 6 * (int)buckets.size() + (n_pml > 0) + 1; }
+    int launches_per_step() const { return 6 * (int)stage_launches().size() + (n_pml > 0) + 1; }
+
+    // ---------------------------------------------------------------- merged form
+    // One persistent launch per RK stage over the jobs of every length the
+    // merged kernel supports (stage_all.cu); other lengths keep their own
+    // launch.  Chosen at create time when it is faster on the scene's own steps.
+    struct StageLaunch {
+        const StageVariant* var;
+        const DevJob* jobs;
+        int n, tw_off, fp, fv, rc;
+        bool all;
+    };
+    struct SepBucket { int b, off, n; };
+    bool merged = false;
+    DevBuf<DevJob> djobs_all, djobs_sep;
+    int n_all = 0;
+    std::vector<SepBucket> sep;
+    DevBuf<int> counters;
+    std::string form_choice;
+
+    std::vector<StageLaunch> stage_launches() const {
+        std::vector<StageLaunch> v;
+        if (merged) {
+            if (n_all > 0) v.push_back({nullptr, djobs_all.p, n_all, 0, 0, 0, 0, true});
+            for (const SepBucket& q : sep) {
+                const Bucket& b = buckets[q.b];
+                v.push_back({b.var, djobs_sep.p + q.off, q.n, b.tw_off, b.fp_off, b.fv_off, b.rc, false});
+            }
+        } else {
+            for (const Bucket& b : buckets) v.push_back({b.var, djobs.p + b.off, b.n, b.tw_off, b.fp_off, b.fv_off, b.rc, false});
+        }
+        return v;
+    }
+
+    bool any_mergeable() const {
+        for (const Bucket& b : buckets)
+            if (merged_supports(b.L) && !b.pinned) return true;
+        return false;
+    }
+
+    // job lists of the merged form: supported lengths (longest first, then the
+    // copy jobs) in one list, the other lengths per bucket
+    void build_merged() {
+        std::vector<DevJob> all, rest;
+        sep.clear();
+        std::vector<int> order;
+        for (size_t i = 0; i < buckets.size(); i++) order.push_back((int)i);
+        std::sort(order.begin(), order.end(), [&](int a, int b) { return buckets[a].L > buckets[b].L; });
+        for (int i : order) {
+            const Bucket& b = buckets[i];
+            if (merged_supports(b.L) && !b.pinned) {
+                auto js = make_jobs(b.L, merged_variant(b.L), false);
+                all.insert(all.end(), js.begin(), js.end());
+            } else {
+                auto js = make_jobs(b.L, b.var, false);
+                sep.push_back({i, (int)rest.size(), (int)js.size()});
+                rest.insert(rest.end(), js.begin(), js.end());
+            }
+        }
+        auto copies = make_jobs(-1, merged_variant(128), true);   // no strips of length -1: the copy jobs only
+        all.insert(all.end(), copies.begin(), copies.end());
+        n_all = (int)all.size();
+        djobs_all.upload(all);
+        djobs_sep.upload(rest);
+        counters.alloc(6);
+        CK(prepare_stage_all());
+        upload_tables();
+        while (side.size() < sep.size() + 1) {
+            cudaStream_t st;
+            CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+            side.push_back(st);
+        }
+    }
+
+    // device time of n steps replayed from the captured graphs (state advances)
+    float time_steps(int n) {
+        cudaEvent_t e0, e1;
+        CK(cudaEventCreate(&e0));
+        CK(cudaEventCreate(&e1));
+        for (int i = 0; i < 2; i++) step(stream);
+        CK(cudaEventRecord(e0, stream));
+        for (int i = 0; i < n; i++) step(stream);
+        CK(cudaEventRecord(e1, stream));
+        CK(cudaEventSynchronize(e1));
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        return ms / n;
+    }
+
+    // per-length launches vs the merged launch: keep the faster (PSTD_MERGED=0/1 forces)
+    void choose_form(bool tune) {
+        int force = -1;
+        if (const char* e = std::getenv("PSTD_MERGED")) force = std::atoi(e) != 0;
+        if (!any_mergeable() || force == 0 || (force < 0 && !tune)) {
+            merged = false;
+            form_choice = "per-length launches";
+            return;
+        }
+        if (force == 1) {
+            build_merged();
+            merged = true;
+            capture_graphs();
+            form_choice = "merged launch (forced)";
+            return;
+        }
+        merged = false;
+        capture_graphs();
+        const float t_len = time_steps(5);
+        reset();
+        build_merged();
+        merged = true;
+        capture_graphs();
+        const float t_all = time_steps(5);
+        reset();
+        char buf[160];
+        std::snprintf(buf, sizeof buf, " (step %.1f us merged vs %.1f us per length)", t_all * 1e3f, t_len * 1e3f);
+        if (t_all >= t_len) {
+            merged = false;
+            capture_graphs();
+            form_choice = std::string("per-length launches") + buf;
+        } else {
+            form_choice = std::string("merged launch") + buf;
+        }
+    }
 
     // Enqueue one time step from set `c` on `st`.  concurrent: the buckets of
     // a stage go on side streams (fork/join); ev (optional): events around
@@ -694,6 +822,7 @@ struct Kernel {
             tmp.push_back(e);
             return e;
         };
+        if (merged) CK(cudaMemsetAsync(counters.p, 0, 6 * sizeof(int), st));   // per-stage job counters
         for (int k = 0; k < 6; k++) {
             cudaEvent_t t0 = nullptr, t1 = nullptr;
             if (ev) {
@@ -701,16 +830,23 @@ struct Kernel {
                 CK(cudaEventCreate(&t1));
                 CK(cudaEventRecord(t0, st));
             }
-            if (concurrent && buckets.size() > 1) {
+            const std::vector<StageLaunch> ls = stage_launches();
+            auto launch = [&](const StageLaunch& l, cudaStream_t s) {
+                if (l.all) {
+                    CK(launch_stage_all(l.n, stage_args(c, k, l.jobs, dtw.p, 0, 0, 0), counters.p + k, s));
+                } else {
+                    StageArgs a = stage_args(c, k, l.jobs, dtw.p + l.tw_off, l.fp, l.fv, l.rc);
+                    CK(l.var->launch(l.n, a, s));
+                }
+            };
+            if (concurrent && ls.size() > 1) {
                 cudaEvent_t fork = mk();
                 CK(cudaEventRecord(fork, st));
                 std::vector<cudaEvent_t> joins;
-                for (size_t i = 0; i < buckets.size(); i++) {
-                    auto& b = buckets[i];
+                for (size_t i = 0; i < ls.size(); i++) {
                     cudaStream_t s = i == 0 ? st : side[i];
                     if (i > 0) CK(cudaStreamWaitEvent(s, fork, 0));
-                    StageArgs a = stage_args(c, k, djobs.p + b.off, dtw.p + b.tw_off, b.fp_off, b.fv_off, b.rc);
-                    CK(b.var->launch(b.n, a, s));
+                    launch(ls[i], s);
                     if (i > 0) {
                         cudaEvent_t j = mk();
                         CK(cudaEventRecord(j, s));
@@ -719,10 +855,7 @@ struct Kernel {
                 }
                 for (auto j : joins) CK(cudaStreamWaitEvent(st, j, 0));
             } else {
-                for (auto& b : buckets) {
-                    StageArgs a = stage_args(c, k, djobs.p + b.off, dtw.p + b.tw_off, b.fp_off, b.fv_off, b.rc);
-                    CK(b.var->launch(b.n, a, st));
-                }
+                for (auto& l : ls) launch(l, st);
             }
             if (ev) {
                 CK(cudaEventRecord(t1, st));

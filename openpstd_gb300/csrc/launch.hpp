@@ -43,6 +43,14 @@ struct StageVariant {
 // all variants compiled for length L (nullptr / 0 if L is not supported)
 int stage_variants(int L, const StageVariant** out);
 
+// merged form (stage_all.cu): one persistent launch per RK stage over the jobs
+// of every length 128..2048; CTAs take jobs from *counter (zeroed before the
+// stage); jobs carry their own length and twiddle-table offset
+bool merged_supports(int L);
+const StageVariant* merged_variant(int L);
+cudaError_t prepare_stage_all();
+cudaError_t launch_stage_all(int n_jobs, const StageArgs& a, int* counter, cudaStream_t st);
+
 cudaError_t launch_pml_post(const int* doms_idx, int n, const DevDomain* doms, float* set, float* fixed, float* p0,
                             const float* att, cudaStream_t st);
 cudaError_t launch_speakers(const DevDomain* doms, const int* x0, const int* y0, int n_dom, const DevSpeaker* spk,

@@ -455,7 +455,7 @@ int pstd_profile_passes(pstd_kernel* h, int32_t n_steps, void* stream, float* ms
         cudaEventDestroy(b);
         if (ms_stage) *ms_stage = ts;
         if (ms_total) *ms_total = tt;
-        if (stage_launches) *stage_launches = (int32_t)(n_steps * 6 * k->buckets.size());
+        if (stage_launches) *stage_launches = (int32_t)(n_steps * 6 * k->stage_launches().size());
         if (total_launches) *total_launches = n_steps * k->launches_per_step();
         return PSTD_OK;
     })
@@ -474,6 +474,7 @@ int pstd_plan_info(pstd_kernel* h, char* buf, int32_t cap) {
     std::string s;
     for (auto& b : h->k->buckets)
         s += "L=" + std::to_string(b.L) + " jobs=" + std::to_string(b.n) + " variant=" + b.var->name + b.choice + "\n";
+    if (!h->k->form_choice.empty()) s += "form: " + h->k->form_choice + "\n";
     if (buf && cap > 0) {
         std::strncpy(buf, s.c_str(), (size_t)cap - 1);
         buf[cap - 1] = 0;

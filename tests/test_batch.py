@@ -32,6 +32,26 @@ def test_batch_equals_alone_bitwise(monkeypatch):
                 assert np.array_equal(b.scene_snapshot(i, d, f), k.snapshot(d, f)), (i, d, f)
 
 
+def test_batch_equals_alone_merged(monkeypatch):
+    """With the merged launch a scene's jobs are the same alone and in a
+    batch: results are bit-identical."""
+    from openpstd_gb300 import kernel
+    from openpstd_gb300.batch import BatchKernel
+    monkeypatch.setenv("PSTD_MERGED", "1")
+    confs = _scenes(4, 30, seed=12)
+    b = BatchKernel(confs)
+    b.advance(30)
+    b.synchronize()
+    for i, c in enumerate(confs):
+        k = kernel.PSTDKernel()
+        k.initialize_kernel(c)
+        k.advance(30)
+        k.synchronize()
+        assert np.array_equal(b.receivers(scene=i), k.receivers()), i
+        for d in range(b.info[i]["domains"]):
+            assert np.array_equal(b.scene_snapshot(i, d, "px"), k.snapshot(d, "px")), (i, d)
+
+
 def test_batch_matches_oracle(oracle_mod):
     from openpstd_gb300.batch import BatchKernel
     confs = _scenes(4, 150, seed=3)

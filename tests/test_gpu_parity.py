@@ -255,3 +255,19 @@ def test_every_stage_variant(oracle_mod, variant, monkeypatch):
     check_parity(oracle_mod, conf, 20, threads=16)
     conf = scenes.rect(7, nx=4100, ny=40, steps=12)    # 8192 (x strips), 128
     check_parity(oracle_mod, conf, 12, threads=16)
+
+
+def test_merged_launch(oracle_mod, monkeypatch):
+    """The merged form -- one persistent launch per RK stage over the strips
+    of every transform length, jobs taken from a per-stage counter --
+    reproduces the oracle."""
+    from openpstd_gb300 import scenes
+    from openpstd_gb300.kernel import PSTDKernel
+    monkeypatch.setenv("PSTD_MERGED", "1")
+    conf = scenes.l_shape(2, scale=0.5, steps=60)      # transform lengths 128, 512, 1024
+    k = PSTDKernel()
+    k.initialize_kernel(conf)
+    assert "merged launch" in k.plan_info()
+    k.close()
+    check_parity(oracle_mod, conf, 60, threads=16)
+    check_parity(oracle_mod, scenes.rect(4, nx=1200, ny=90, steps=30), 30, threads=16)   # 2048, 256, 128
