@@ -32,7 +32,6 @@ __device__ __noinline__ void merged_job(float2* sm, const StageArgs& A, int j, i
     const DevJob job = A.jobs[j];
     const DevDomain dom = A.doms[job.dom];
     const bool first = A.first_step[dom.scene] != 0;
-    prefetch_job<C, MERGED_NT>(A, job, dom, first, tid);
     gather<C, MERGED_NT, false>(sm, A, job, dom, first, tid);
     __syncthreads();
     const bool vel = job.kind & JK_VEL;

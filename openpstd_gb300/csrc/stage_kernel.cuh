@@ -629,7 +629,6 @@ __device__ __forceinline__ float4 ldf4(const float* p) {   // p 16-byte aligned
         : "l"(p));
     return v;
 }
-__device__ __forceinline__ void prefetch_l2(const float* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 
 // Source of the strip data of one domain in one stage.
 struct Src {
@@ -881,53 +880,6 @@ __device__ __forceinline__ void gather(float2* sm, const StageArgs& A, const Dev
     else gather_k<C, NTH, ZERO, false>(sm, A, job, dom, first, S, tid);
 }
 
-// ---- L2 prefetch of everything a job streams: the strip rows / columns of
-// the gather and the stage-start values the epilogue reads (128-byte lines;
-// rows start on line boundaries, so every line touched lies inside its row)
-template <class C, int NTH>
-__device__ __forceinline__ void prefetch_job(const StageArgs& A, const DevJob& job, const DevDomain& dom, bool first,
-                                             int tid) {
-    const bool vel = job.kind & JK_VEL;
-    const bool ydir = job.kind & JK_Y;
-    const int n = (ydir ? dom.ny : dom.nx) + (vel ? 1 : 0);
-    const int nout = vel ? n - 1 : n + 1;
-    const Src S = strip_source(A, dom, vel, ydir, first);
-    long long fo;
-    int fp;
-    if (!vel) { fo = ydir ? dom.o_vy : dom.o_vx; fp = ydir ? dom.pitch_vy : dom.pitch_vx; }
-    else { fo = ydir ? dom.o_py : dom.o_px; fp = dom.pitch_p; }
-    const float* P = A.prev + fo;
-    const int count = job.count;
-    if (!ydir) {
-        const int li = (n + 31) >> 5, lo = (nout + 31) >> 5;
-        const int nin = S.b ? 2 * li : li, per_row = nin + lo;
-        for (int k = tid; k < count * per_row; k += NTH) {
-            const int s = k / per_row, l = k - s * per_row;
-            const long long row = job.first + s;
-            if (l < li) prefetch_l2(S.a + row * S.pitch + 32 * l);
-            else if (l < nin) prefetch_l2(S.b + row * S.pitch + 32 * (l - li));
-            else prefetch_l2(P + row * fp + 32 * (l - nin));
-        }
-    } else {
-        // the count-float segment of a row spans one line, or two
-        const int c0 = job.first, c1 = job.first + count - 1;
-        const bool two = (c0 >> 5) != (c1 >> 5);
-        for (int i = tid; i < n; i += NTH) {
-            const long long e = (long long)i * S.pitch;
-            prefetch_l2(S.a + e + c0);
-            if (two) prefetch_l2(S.a + e + c1);
-            if (S.b) {
-                prefetch_l2(S.b + e + c0);
-                if (two) prefetch_l2(S.b + e + c1);
-            }
-        }
-        for (int i = tid; i < nout; i += NTH) {
-            prefetch_l2(P + (long long)i * fp + c0);
-            if (two) prefetch_l2(P + (long long)i * fp + c1);
-        }
-    }
-}
-
 // ---- step 5: slice, RK update, (sixth stage) PML on vx / vy
 // RK update of one value in the reference's operation order
 // (kernel/Solver.cpp:174-181): v0 - (dt*a_k) * (L / rho) and p0 - (dt*a_k) * ((L*rho)*c^2)
@@ -1098,7 +1050,6 @@ __global__ void __launch_bounds__(C::NT, C::MINB) stage_kernel(StageArgs A) {
         return;
     }
     const bool first = A.first_step[dom.scene] != 0;
-    prefetch_job<C, C::NT>(A, job, dom, first, threadIdx.x);
     constexpr bool PRUNE = !C::TC;   // the tensor-core passes read the padding
     gather<C, C::NT, !PRUNE>(sm, A, job, dom, first, threadIdx.x);
     __syncthreads();
