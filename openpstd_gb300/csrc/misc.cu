@@ -29,29 +29,30 @@ int stage_variants(int L, const StageVariant** out) {
 // domains (fields in the fixed buffer) get all four multiplies here.
 __global__ void pml_post_kernel(const int* idx, const DevDomain* doms, float* set, float* fixed, float* p0,
                                 const float* __restrict__ att) {
+    // rows over blockIdx.x (grid stride), columns over the threads: no division
     const DevDomain d = doms[idx[blockIdx.y]];
     float* base = d.fixed ? fixed : set;
-    const int stride = gridDim.x * blockDim.x;
-    const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
-    for (int k = t0; k < d.nx * d.ny; k += stride) {
-        const int r = k / d.nx, i = k - r * d.nx;
-        const long long e = (long long)r * d.pitch_p + i;
-        const float px = base[d.o_px + e], py = base[d.o_py + e];
-        p0[d.o_p0 + e] = __fadd_rn(px, py);
-        if (d.att_xp >= 0) base[d.o_px + e] = __fmul_rn(px, att[d.att_xp + i]);
-        if (d.att_yp >= 0) base[d.o_py + e] = __fmul_rn(py, att[d.att_yp + r]);
+    for (int r = blockIdx.x; r < d.ny; r += gridDim.x) {
+        const float ay = d.att_yp >= 0 ? att[d.att_yp + r] : 1.f;
+        for (int i = threadIdx.x; i < d.nx; i += blockDim.x) {
+            const long long e = (long long)r * d.pitch_p + i;
+            const float px = base[d.o_px + e], py = base[d.o_py + e];
+            p0[d.o_p0 + e] = __fadd_rn(px, py);
+            if (d.att_xp >= 0) base[d.o_px + e] = __fmul_rn(px, att[d.att_xp + i]);
+            if (d.att_yp >= 0) base[d.o_py + e] = __fmul_rn(py, ay);
+        }
     }
     if (d.fixed) {
-        for (int k = t0; k < d.ny * (d.nx + 1); k += stride) {
-            const int r = k / (d.nx + 1), i = k - r * (d.nx + 1);
-            const long long e = d.o_vx + (long long)r * d.pitch_vx + i;
-            if (d.att_xv >= 0) base[e] = __fmul_rn(base[e], att[d.att_xv + i]);
-        }
-        for (int k = t0; k < (d.ny + 1) * d.nx; k += stride) {
-            const int r = k / d.nx, i = k - r * d.nx;
-            const long long e = d.o_vy + (long long)r * d.pitch_vy + i;
-            if (d.att_yv >= 0) base[e] = __fmul_rn(base[e], att[d.att_yv + r]);
-        }
+        for (int r = blockIdx.x; r < d.ny; r += gridDim.x)
+            for (int i = threadIdx.x; i < d.nx + 1; i += blockDim.x) {
+                const long long e = d.o_vx + (long long)r * d.pitch_vx + i;
+                if (d.att_xv >= 0) base[e] = __fmul_rn(base[e], att[d.att_xv + i]);
+            }
+        for (int r = blockIdx.x; r < d.ny + 1; r += gridDim.x)
+            for (int i = threadIdx.x; i < d.nx; i += blockDim.x) {
+                const long long e = d.o_vy + (long long)r * d.pitch_vy + i;
+                if (d.att_yv >= 0) base[e] = __fmul_rn(base[e], att[d.att_yv + r]);
+            }
     }
 }
 
@@ -123,18 +124,17 @@ __global__ void frame_kernel(const int* idx, const long long* dst_off, const Dev
     const DevDomain d = doms[idx[blockIdx.y]];
     float* out = dst + dst_off[blockIdx.y];
     const int mx = (d.nx + sub - 1) / sub, my = (d.ny + sub - 1) / sub;
-    const int stride = gridDim.x * blockDim.x;
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < mx * my; k += stride) {
-        const int r = k / mx, i = k - r * mx;
-        const long long e = (long long)r * sub * d.pitch_p + (long long)i * sub;
-        out[k] = __fadd_rn(set[d.o_px + e], set[d.o_py + e]);
-    }
+    for (int r = blockIdx.x; r < my; r += gridDim.x)
+        for (int i = threadIdx.x; i < mx; i += blockDim.x) {
+            const long long e = (long long)r * sub * d.pitch_p + (long long)i * sub;
+            out[(long long)r * mx + i] = __fadd_rn(set[d.o_px + e], set[d.o_py + e]);
+        }
 }
 
 cudaError_t launch_pml_post(const int* idx, int n, const DevDomain* doms, float* set, float* fixed, float* p0,
                             const float* att, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    pml_post_kernel<<<dim3(8, n), 256, 0, st>>>(idx, doms, set, fixed, p0, att);
+    pml_post_kernel<<<dim3(128, n), 128, 0, st>>>(idx, doms, set, fixed, p0, att);
     return cudaGetLastError();
 }
 
@@ -161,7 +161,7 @@ cudaError_t launch_server_receivers(const DevSrvReceiver* rec, int n_rec, const 
 cudaError_t launch_frame(const int* idx, const long long* dst_off, int n, const DevDomain* doms, const float* set,
                          float* dst, cudaStream_t st, int sub) {
     if (n <= 0) return cudaSuccess;
-    frame_kernel<<<dim3(64, n), 256, 0, st>>>(idx, dst_off, doms, set, dst, sub);
+    frame_kernel<<<dim3(128, n), 128, 0, st>>>(idx, dst_off, doms, set, dst, sub);
     return cudaGetLastError();
 }
 

@@ -732,10 +732,10 @@ __device__ __forceinline__ void gather_k(float2* sm, const StageArgs& A, const D
             const float* a0 = S.a + (long long)(job.first + s0) * S.pitch;
             const float* b0 = TWO ? S.b + (long long)(job.first + s0) * S.pitch : nullptr;
             const bool h0 = s0 < count, h1 = s0 + 1 < count;
-            for (int c0 = (warp % WPP) * 32 + lane; c0 < chunks; c0 += 4 * WPP * 32) {
+            for (int c0 = (warp % WPP) * 32 + lane; c0 < chunks; c0 += 2 * WPP * 32) {
                 float4 u[4], v[4];
 #pragma unroll
-                for (int q = 0; q < 4; q++) {
+                for (int q = 0; q < 2; q++) {
                     const int c = c0 + q * WPP * 32, i = c << 2;
                     u[q] = v[q] = make_float4(0.f, 0.f, 0.f, 0.f);
                     if (c < chunks) {
@@ -745,7 +745,7 @@ __device__ __forceinline__ void gather_k(float2* sm, const StageArgs& A, const D
                     }
                 }
 #pragma unroll
-                for (int q = 0; q < 4; q++) {
+                for (int q = 0; q < 2; q++) {
                     const int c = c0 + q * WPP * 32, i = c << 2;
                     if (c < chunks) {
                         float2* d = sm + cs * SP + W + i;
