@@ -626,14 +626,19 @@ struct Kernel {
                         continue;
                     }
                     CK(vs[i].launch((int)all[i].size(), a, stream));
-                    CK(cudaEventRecord(e0, stream));
+                    // best of three trials of five launches (variants often differ by a
+                    // few percent; one trial lets noise pick)
                     const int reps = 5;
-                    for (int w = 0; w < reps; w++) CK(vs[i].launch((int)all[i].size(), a, stream));
-                    CK(cudaEventRecord(e1, stream));
-                    CK(cudaEventSynchronize(e1));
-                    float ms;
-                    CK(cudaEventElapsedTime(&ms, e0, e1));
-                    ms /= reps;
+                    float ms = 1e30f;
+                    for (int trial = 0; trial < 3; trial++) {
+                        CK(cudaEventRecord(e0, stream));
+                        for (int w = 0; w < reps; w++) CK(vs[i].launch((int)all[i].size(), a, stream));
+                        CK(cudaEventRecord(e1, stream));
+                        CK(cudaEventSynchronize(e1));
+                        float t;
+                        CK(cudaEventElapsedTime(&t, e0, e1));
+                        ms = std::min(ms, t / reps);
+                    }
                     char buf[64];
                     std::snprintf(buf, sizeof buf, " %d:%.1fus", i, ms * 1e3f);
                     rec += buf;
