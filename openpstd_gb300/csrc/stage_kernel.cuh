@@ -1314,12 +1314,11 @@ __device__ __forceinline__ void pipe_blend(float2* sm, const float* slot, const 
     }
 }
 
-// slice, RK update against the staged stage-start values, store
+// slice, RK update against the staged stage-start values sp, store
 template <class C, int NTH>
-__device__ __forceinline__ void pipe_epilogue(const float2* sm, const float* slot, const StageArgs& A, const DevJob& job,
+__device__ __forceinline__ void pipe_epilogue(const float2* sm, const float* sp, const StageArgs& A, const DevJob& job,
                                               const DevDomain& dom, const PipeJob& g, int rc, int tid) {
     constexpr int CS = C::CS, SP = C::SP, S2 = 2 * CS;
-    const float* sp = slot + 2 * S2 * rc;
     float* __restrict__ out = A.out;
     const float cdt = A.doms[job.dom].cdt[A.stage];
     const float rho = dom.rho, c2 = dom.c2, rinv = __frcp_rn(rho);
@@ -1405,7 +1404,7 @@ __global__ void __launch_bounds__(C::NT, C::MINB) stage_pipe(StageArgs A, int n_
             __syncthreads();
             convolve<C, NT, 0, false>(sm, A.tw, A.filt + job.dtab, tid);
             __syncthreads();
-            pipe_epilogue<C, NT>(sm, slot, A, job, dom, g, rc, tid);
+            pipe_epilogue<C, NT>(sm, slot + 2 * S2 * rc, A, job, dom, g, rc, tid);
         }
         __syncthreads();   // the slot and the FFT buffer are free again
         if (k + 2 < mine) {
@@ -1414,6 +1413,105 @@ __global__ void __launch_bounds__(C::NT, C::MINB) stage_pipe(StageArgs A, int n_
         }
         cp_commit();
     }
+}
+
+// ---------------------------------------------------------------- staged stage-start form
+// The plain kernel's steps, with the stage-start values of the updated field
+// (the only global reads of the epilogue) copied to shared memory by cp.async
+// at the start of the job: they arrive while the strips are gathered and
+// transformed, and the epilogue no longer waits on global memory.  Shared
+// memory: the FFT buffer, then S2 x rc floats (rows of x jobs; [rc][S2] for y
+// jobs, the layout of the pipelined form's P slot).
+template <class C, int NTH>
+__device__ __forceinline__ void stage_prev_in(float* sp, const StageArgs& A, const DevJob& job, const PipeJob& g,
+                                              int rc, int tid) {
+    constexpr int S2 = 2 * C::CS;
+    const float* P = A.prev + g.fo;
+    if (!g.ydir) {
+        const int qp = (g.nout + 3) >> 2;   // whole quads: rows are padded past their last quad
+        for (int k = tid; k < g.count * qp; k += NTH) {
+            const int s = k / qp, q = k - s * qp;
+            cp16(sp + s * rc + 4 * q, P + (long long)(job.first + s) * g.fp + 4 * q);
+        }
+    } else if (g.vec) {
+        constexpr int G = S2 / 4;
+        for (int k = tid; k < g.nout * G; k += NTH) {
+            const int q = k % G, i = k / G;
+            cp16(sp + i * S2 + 4 * q, P + (long long)i * g.fp + job.first + 4 * q);
+        }
+    } else {
+        for (int k = tid; k < g.nout * g.count; k += NTH) {
+            const int s = k % g.count, i = k / g.count;
+            cp4(sp + i * S2 + s, P + (long long)i * g.fp + job.first + s);
+        }
+    }
+}
+
+template <class C>
+__global__ void __launch_bounds__(C::NT, C::MINB) stage_sprev(StageArgs A) {
+    extern __shared__ float2 sm[];
+    constexpr int S2 = 2 * C::CS;
+    const int rc = A.row_cap;
+    float* sp = reinterpret_cast<float*>(sm + C::BUF);
+    const DevJob job = A.jobs[blockIdx.x];
+    const DevDomain dom = A.doms[job.dom];
+    if (job.kind & JK_COPY) {
+        copy_axis<C::NT>(A, dom, job.kind & JK_Y, threadIdx.x);
+        return;
+    }
+    const bool first = A.first_step[dom.scene] != 0;
+    const PipeJob g = pipe_job<S2>(A, job, dom, first);
+    stage_prev_in<C, C::NT>(sp, A, job, g, rc, threadIdx.x);
+    cp_commit();
+    gather<C, C::NT, false>(sm, A, job, dom, first, threadIdx.x);
+    __syncthreads();
+    convolve<C, C::NT, 0, false, true>(sm, A.tw, A.filt + job.dtab, threadIdx.x, 2 * job.W + g.n, job.W,
+                                       job.W + g.nout);
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    __syncthreads();
+    pipe_epilogue<C, C::NT>(sm, sp, A, job, dom, g, rc, threadIdx.x);
+}
+
+template <class C>
+size_t sprev_smem(int rc) {
+    return (size_t)C::BUF * 8 + (size_t)2 * C::CS * rc * 4;
+}
+
+template <class C>
+cudaError_t launch_sprev_t(int n_jobs, const StageArgs& a, cudaStream_t st) {
+    static int optin = 0;
+    if (optin == 0) {
+        int dev;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    }
+    const size_t smem = sprev_smem<C>(a.row_cap);
+    if (a.row_cap < 4 || (a.row_cap & 3) || smem > (size_t)optin) return cudaErrorInvalidValue;   // does not fit
+    stage_sprev<C><<<n_jobs, C::NT, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <class C>
+cudaError_t prepare_sprev_t() {
+    int dev, optin;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    return cudaFuncSetAttribute(stage_sprev<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+}
+
+template <class C>
+StageVariant make_sprev_variant(const char* name) {
+    StageVariant v;
+    v.L = C::L; v.CS = C::CS; v.NT = C::NT; v.smem = 0; v.np = C::NP;
+    v.r[0] = C::R0; v.r[1] = C::R1; v.r[2] = C::R2; v.r[3] = C::R3;
+    v.persistent = false;
+    v.pipe = true;   // needs the bucket's row cap
+    v.bf16 = false;
+    v.launch = &launch_sprev_t<C>;
+    v.prepare = &prepare_sprev_t<C>;
+    v.smem_for = &sprev_smem<C>;
+    v.name = name;
+    return v;
 }
 
 template <class C>

@@ -14,9 +14,11 @@ const StageVariant* stage_variants_large(int L, int* n) {
         make_pipe_variant<Cfg<2048, 1, 128, 2, 16, 16, 8>>("L2048 cs1 pipe128 r16.16.8"),
         make_variant<Cfg<2048, 4, 512, 2, 16, 16, 8>>("L2048 cs4 nt512 mb2 r16.16.8"),
         make_variant<Cfg<2048, 2, 256, 4, 16, 16, 8>>("L2048 cs2 nt256 mb4 r16.16.8"),
+        make_sprev_variant<Cfg<2048, 4, 256, 2, 16, 16, 8>>("L2048 cs4 nt256 sprev r16.16.8"),
+        make_sprev_variant<Cfg<2048, 2, 256, 4, 16, 16, 8>>("L2048 cs2 nt256 mb4 sprev r16.16.8"),
     };
     switch (L) {
-        case 2048: *n = 9; return v2048;
+        case 2048: *n = 11; return v2048;
         default: *n = 0; return nullptr;
     }
 }

@@ -11,6 +11,7 @@ const StageVariant* stage_variants_mid(int L, int* n) {
         make_pipe_variant<Cfg<512, 4, 128, 2, 8, 8, 8>>("L512 cs4 pipe128 r8.8.8"),
         make_variant<Cfg<512, 8, 256, 4, 8, 8, 8>>("L512 cs8 nt256 mb4 r8.8.8"),
         make_variant<Cfg<512, 8, 128, 4, 32, 16>>("L512 cs8 nt128 mb4 r32.16"),
+        make_sprev_variant<Cfg<512, 8, 256, 3, 8, 8, 8>>("L512 cs8 nt256 sprev r8.8.8"),
     };
     static const StageVariant v1024[] = {
         make_variant<Cfg<1024, 8, 256, 3, 16, 8, 8>>("L1024 cs8 nt256 r16.8.8"),
@@ -24,10 +25,13 @@ const StageVariant* stage_variants_mid(int L, int* n) {
         make_variant<Cfg<1024, 2, 128, 8, 16, 8, 8>>("L1024 cs2 nt128 mb8 r16.8.8"),
         make_variant<Cfg<1024, 4, 128, 4, 32, 32>>("L1024 cs4 nt128 mb4 r32.32"),
         make_variant<Cfg<1024, 8, 256, 2, 32, 32>>("L1024 cs8 nt256 mb2 r32.32"),
+        make_sprev_variant<Cfg<1024, 4, 256, 3, 16, 8, 8>>("L1024 cs4 nt256 sprev r16.8.8"),
+        make_sprev_variant<Cfg<1024, 4, 256, 4, 16, 8, 8>>("L1024 cs4 nt256 mb4 sprev r16.8.8"),
+        make_sprev_variant<Cfg<1024, 8, 256, 2, 32, 32>>("L1024 cs8 nt256 mb2 sprev r32.32"),
     };
     switch (L) {
-        case 512: *n = 6; return v512;
-        case 1024: *n = 11; return v1024;
+        case 512: *n = 7; return v512;
+        case 1024: *n = 14; return v1024;
         default: *n = 0; return nullptr;
     }
 }
