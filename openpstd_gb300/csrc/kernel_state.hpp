@@ -130,6 +130,7 @@ struct Bucket {
     int fp_off = 0, fv_off = 0;    // float2 offsets of the pressure / velocity filters
     int rc = 4;                    // floats staged per strip by the pipelined form
     bool pinned = false;           // variant fixed by PSTD_PLAN / PSTD_DFT: not tuned
+    std::vector<const StageVariant*> cands;   // fastest variants timed alone (refined on whole steps)
     std::string choice;            // autotune record
 };
 
@@ -542,6 +543,10 @@ struct Kernel {
             CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
             side.push_back(s);
         }
+        if (autotune) {
+            refine_plan();
+            reset();
+        }
         choose_form(autotune);
         if (!merged) capture_graphs();
         std::string choice;
@@ -612,6 +617,7 @@ struct Kernel {
                 float best = 1e30f;
                 int best_i = 0;
                 std::string rec;
+                std::vector<std::pair<float, int>> timed;
                 cudaEvent_t e0, e1;
                 CK(cudaEventCreate(&e0));
                 CK(cudaEventCreate(&e1));
@@ -643,11 +649,15 @@ struct Kernel {
                     std::snprintf(buf, sizeof buf, " %d:%.1fus", i, ms * 1e3f);
                     rec += buf;
                     if (ms < best) { best = ms; best_i = i; }
+                    timed.push_back({ms, i});
                 }
                 cudaEventDestroy(e0);
                 cudaEventDestroy(e1);
                 b.var = &vs[best_i];
                 b.choice = " tuned" + rec;
+                std::sort(timed.begin(), timed.end());
+                b.cands.clear();
+                for (size_t q = 0; q < timed.size() && q < 3; q++) b.cands.push_back(&vs[timed[q].second]);
             }
         }
         std::vector<DevJob> jobs;
@@ -776,6 +786,38 @@ struct Kernel {
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         return ms / n;
+    }
+
+    // The isolated timing of plan() ranks each length alone, but a step runs
+    // all lengths concurrently: one pass of coordinate descent over each
+    // length's three fastest variants, timed on whole captured steps (the
+    // state advances; the caller resets it).
+    void refine_plan() {
+        std::vector<size_t> order;
+        for (size_t i = 0; i < buckets.size(); i++)
+            if (buckets[i].cands.size() > 1) order.push_back(i);
+        if (order.empty()) return;
+        plan(false);
+        capture_graphs();
+        float best = time_steps(4);
+        for (size_t i : order) {
+            Bucket& b = buckets[i];
+            const StageVariant* keep = b.var;
+            for (const StageVariant* v : b.cands) {
+                if (v == keep) continue;
+                b.var = v;
+                plan(false);
+                capture_graphs();
+                const float t = time_steps(4);
+                if (t < best) { best = t; keep = v; }
+            }
+            if (b.var != keep) {
+                b.var = keep;
+                plan(false);
+            }
+            if (b.var != b.cands[0]) b.choice += std::string(" refined on whole steps: ") + b.var->name;
+        }
+        capture_graphs();
     }
 
     // per-length launches vs the merged launch: keep the faster (PSTD_MERGED=0/1 forces)
