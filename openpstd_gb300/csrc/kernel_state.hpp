@@ -657,7 +657,7 @@ struct Kernel {
                 b.choice = " tuned" + rec;
                 std::sort(timed.begin(), timed.end());
                 b.cands.clear();
-                for (size_t q = 0; q < timed.size() && q < 3; q++) b.cands.push_back(&vs[timed[q].second]);
+                for (size_t q = 0; q < timed.size() && q < 8; q++) b.cands.push_back(&vs[timed[q].second]);
             }
         }
         std::vector<DevJob> jobs;
