@@ -113,7 +113,9 @@ typedef struct pstd_callbacks {
 typedef struct pstd_kernel pstd_kernel;
 
 /* Build the scene (domains, automatic PML, speakers, receivers, attenuation
- * tables) on the host and upload it to device 0.
+ * tables) on the host and upload it to device 0.  The stage-kernel plan is
+ * autotuned (PSTD_AUTOTUNE=0 disables it) at the first create of a scene
+ * structure in the process and taken from a per-process plan cache afterwards.
  * Replaces PSTDKernel::initialize_kernel (kernel/PSTDKernel.cpp:49-70). */
 int pstd_create(const pstd_config* config, const pstd_callbacks* log_cb, pstd_kernel** out);
 
@@ -213,8 +215,8 @@ int pstd_scene_attenuation(pstd_kernel* k, int32_t index, float* ax_p, float* ax
 
 /* ---- timing of the stage kernels (no reference counterpart) ------------ */
 /* Advance n_steps with CUDA events around every RK stage (its strip-length
- * buckets launched back to back); returns the summed device time [ms] of the
- * stage-kernel launches, the time of the whole region, and the launch counts.
+ * launches concurrent, as in the step graphs); returns the summed device time
+ * [ms] of the stages, the time of the whole region, and the launch counts.
  * Results are identical to pstd_advance. */
 int pstd_profile_passes(pstd_kernel* k, int32_t n_steps, void* stream,
                         float* ms_stage, float* ms_total, int32_t* stage_launches, int32_t* total_launches);

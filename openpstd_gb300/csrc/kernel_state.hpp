@@ -12,6 +12,7 @@
 #include <cstring>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 #include <tuple>
@@ -120,6 +121,23 @@ inline int planned_variant(int L) {
         at = end + 1;
     }
     return -1;
+}
+
+// Plans chosen by the autotuner, kept per process and keyed by the scene's
+// strip-job structure (like the reference's WisdomCache for FFT plans): a scene
+// tuned once is created again without timing.
+struct PlanChoice {
+    std::vector<std::pair<int, const StageVariant*>> vars;   // (L, variant)
+    bool merged = false;
+    std::string form;
+};
+inline std::mutex& plan_cache_mutex() {
+    static std::mutex m;
+    return m;
+}
+inline std::map<std::string, PlanChoice>& plan_cache() {
+    static std::map<std::string, PlanChoice> c;
+    return c;
 }
 
 struct Bucket {
@@ -534,20 +552,49 @@ struct Kernel {
         dframe_off.upload(frame_off);
         dframe.alloc(std::max<size_t>(frame_floats, 1));
 
-        // ---- tables and the job plan (autotuned), then the launch form
-        reset();
-        plan(autotune);
-        reset();
+        // ---- tables and the job plan (autotuned, or from the plan cache), then the launch form
         for (size_t i = 0; i < buckets.size(); i++) {
             cudaStream_t s;
             CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
             side.push_back(s);
         }
+        const std::string sig = autotune ? plan_signature() : std::string();
+        PlanChoice cached;
+        bool hit = false;
         if (autotune) {
-            refine_plan();
-            reset();
+            std::lock_guard<std::mutex> lock(plan_cache_mutex());
+            auto it = plan_cache().find(sig);
+            if (it != plan_cache().end()) { cached = it->second; hit = true; }
         }
-        choose_form(autotune);
+        reset();
+        if (hit) {
+            for (auto& b : buckets)
+                for (auto& lv : cached.vars)
+                    if (lv.first == b.L) { b.var = lv.second; b.choice = " (plan cache)"; }
+            plan(false);
+            if (cached.merged) {
+                build_merged();
+                merged = true;
+                capture_graphs();
+            }
+            form_choice = cached.form + " (plan cache)";
+        } else {
+            plan(autotune);
+            reset();
+            if (autotune) {
+                refine_plan();
+                reset();
+            }
+            choose_form(autotune);
+            if (autotune) {
+                PlanChoice pc;
+                for (auto& b : buckets) pc.vars.push_back({b.L, b.var});
+                pc.merged = merged;
+                pc.form = form_choice;
+                std::lock_guard<std::mutex> lock(plan_cache_mutex());
+                plan_cache()[sig] = pc;
+            }
+        }
         if (!merged) capture_graphs();
         std::string choice;
         for (auto& b : buckets) choice += " [" + std::string(b.var->name) + b.choice + "]";
@@ -786,6 +833,23 @@ struct Kernel {
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         return ms / n;
+    }
+
+    // the strip-job structure of the scenes (domain sizes and kinds, every strip
+    // run with its neighbours and transform length): equal signatures get
+    // equal job lists for every variant
+    std::string plan_signature() const {
+        std::string s;
+        auto put = [&](long long v) { s += std::to_string(v); s += ','; };
+        for (const Scene& sc : scenes) {
+            put((long long)sc.doms.size());
+            for (const Domain& d : sc.doms) { put(d.nx); put(d.ny); put(d.rigid); put(d.pml); put(d.update[0]); put(d.update[1]); }
+            for (const StripRun& r : sc.runs) {
+                put(r.dom); put(r.axis); put(r.first); put(r.count); put(r.d1); put(r.d2); put(run_length(sc, r));
+            }
+            s += ';';
+        }
+        return s;
     }
 
     // The isolated timing of plan() ranks each length alone, but a step runs

@@ -436,7 +436,7 @@ int pstd_profile_passes(pstd_kernel* h, int32_t n_steps, void* stream, float* ms
         CK(cudaEventCreate(&b));
         CK(cudaEventRecord(a, st));
         for (int i = 0; i < n_steps; i++) {
-            k->enqueue_step(k->cur, st, false, &ev);
+            k->enqueue_step(k->cur, st, true, &ev);   // lengths concurrent, as in the step graphs
             k->cur = (k->cur + 2) % 3;
             k->steps++;
         }
