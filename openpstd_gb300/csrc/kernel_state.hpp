@@ -558,10 +558,12 @@ struct Kernel {
             CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
             side.push_back(s);
         }
-        const std::string sig = autotune ? plan_signature() : std::string();
+        // the cache serves unforced plans only (PSTD_MERGED / PSTD_PLAN / PSTD_DFT pin choices)
+        const bool cacheable = autotune && !std::getenv("PSTD_MERGED") && !std::getenv("PSTD_PLAN") && !want_bf16_dft();
+        const std::string sig = cacheable ? plan_signature() : std::string();
         PlanChoice cached;
         bool hit = false;
-        if (autotune) {
+        if (cacheable) {
             std::lock_guard<std::mutex> lock(plan_cache_mutex());
             auto it = plan_cache().find(sig);
             if (it != plan_cache().end()) { cached = it->second; hit = true; }
@@ -586,7 +588,7 @@ struct Kernel {
                 reset();
             }
             choose_form(autotune);
-            if (autotune) {
+            if (cacheable) {
                 PlanChoice pc;
                 for (auto& b : buckets) pc.vars.push_back({b.L, b.var});
                 pc.merged = merged;
