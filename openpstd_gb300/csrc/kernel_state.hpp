@@ -129,6 +129,7 @@ inline int planned_variant(int L) {
 struct PlanChoice {
     std::vector<std::pair<int, const StageVariant*>> vars;   // (L, variant)
     bool merged = false;
+    bool longest_first = false;
     std::string form;
 };
 inline std::mutex& plan_cache_mutex() {
@@ -574,6 +575,7 @@ struct Kernel {
                 for (auto& lv : cached.vars)
                     if (lv.first == b.L) { b.var = lv.second; b.choice = " (plan cache)"; }
             plan(false);
+            longest_first = cached.longest_first;
             if (cached.merged) {
                 build_merged();
                 merged = true;
@@ -591,6 +593,7 @@ struct Kernel {
             if (cacheable) {
                 PlanChoice pc;
                 for (auto& b : buckets) pc.vars.push_back({b.L, b.var});
+                pc.longest_first = longest_first;
                 pc.merged = merged;
                 pc.form = form_choice;
                 std::lock_guard<std::mutex> lock(plan_cache_mutex());
@@ -760,6 +763,7 @@ struct Kernel {
     };
     struct SepBucket { int b, off, n; };
     bool merged = false;
+    bool longest_first = false;   // launch order of the lengths in a stage (buckets ascend in L)
     DevBuf<DevJob> djobs_all, djobs_sep;
     int n_all = 0;
     std::vector<SepBucket> sep;
@@ -776,6 +780,7 @@ struct Kernel {
             }
         } else {
             for (const Bucket& b : buckets) v.push_back({b.var, djobs.p + b.off, b.n, b.tw_off, b.fp_off, b.fv_off, b.rc, false});
+            if (longest_first) std::reverse(v.begin(), v.end());
         }
         return v;
     }
@@ -883,6 +888,10 @@ struct Kernel {
             }
             if (b.var != b.cands[0]) b.choice += std::string(" refined on whole steps: ") + b.var->name;
         }
+        // launch order: longest transforms first or last (their CTAs run longest)
+        longest_first = true;
+        capture_graphs();
+        if (time_steps(4) >= best) longest_first = false;
         capture_graphs();
     }
 

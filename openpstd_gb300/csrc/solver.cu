@@ -475,6 +475,7 @@ int pstd_plan_info(pstd_kernel* h, char* buf, int32_t cap) {
     for (auto& b : h->k->buckets)
         s += "L=" + std::to_string(b.L) + " jobs=" + std::to_string(b.n) + " variant=" + b.var->name + b.choice + "\n";
     if (!h->k->form_choice.empty()) s += "form: " + h->k->form_choice + "\n";
+    if (h->k->longest_first) s += "order: longest transforms launched first\n";
     if (buf && cap > 0) {
         std::strncpy(buf, s.c_str(), (size_t)cap - 1);
         buf[cap - 1] = 0;
