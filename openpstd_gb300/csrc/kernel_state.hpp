@@ -182,6 +182,16 @@ struct Kernel {
     DevBuf<float> dwin, datt;
     DevBuf<int> dpml;                 // indices of PML domains
     int n_pml = 0;
+    int pml_blocks = 0;               // grid of the PML post kernel
+    DevBuf<int> dpml_off;             // prefix sums of its blocks per PML domain
+
+    // one block per (row, 128-column chunk) of every PML domain, in one flat grid
+    void set_pml_blocks(const std::vector<int>& pml) {
+        std::vector<int> off{0};
+        for (int k : pml) off.push_back(off.back() + (hdoms[k].ny + 1) * ((hdoms[k].nx + 1 + 127) >> 7));
+        pml_blocks = off.back();
+        dpml_off.upload(off);
+    }
     DevBuf<DevReceiver> drec;
     DevBuf<float> dring;
     DevBuf<int> dcounter;
@@ -463,6 +473,7 @@ struct Kernel {
         datt.upload(att);
         n_pml = (int)pml_idx.size();
         dpml.upload(pml_idx);
+        set_pml_blocks(pml_idx);
         ddoms.upload(hdoms);
 
         // ---- buckets
@@ -984,7 +995,8 @@ struct Kernel {
                 ev->push_back({t0, t1});
             }
         }
-        if (n_pml > 0) CK(launch_pml_post(dpml.p, n_pml, ddoms.p, sets[B].p, fixed.p, p0.p, datt.p, st));
+        if (n_pml > 0)
+            CK(launch_pml_post(dpml.p, n_pml, pml_blocks, ddoms.p, sets[B].p, fixed.p, p0.p, datt.p, st, dpml_off.p));
         if (srv.on) {
             CK(cudaMemsetAsync(first_step.p, 0, srv.n_flags * sizeof(int), st));
             CK(launch_server_receivers(srv.rec, n_rec, ddoms.p, sets[B].p, srv.aux, srv.scene_step, srv.slots,

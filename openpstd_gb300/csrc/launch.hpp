@@ -51,8 +51,11 @@ const StageVariant* merged_variant(int L);
 cudaError_t prepare_stage_all();
 cudaError_t launch_stage_all(int n_jobs, const StageArgs& a, int* counter, cudaStream_t st);
 
-cudaError_t launch_pml_post(const int* doms_idx, int n, const DevDomain* doms, float* set, float* fixed, float* p0,
-                            const float* att, cudaStream_t st);
+// one block per (row, 128-column chunk): with off (n + 1 prefix sums of the
+// domains' (rows + 1) x ceil((columns + 1) / 128) block counts) blocks is their
+// total; without, blocks is the count of the largest domain (grid blocks x n)
+cudaError_t launch_pml_post(const int* doms_idx, int n, int blocks, const DevDomain* doms, float* set, float* fixed,
+                            float* p0, const float* att, cudaStream_t st, const int* off = nullptr);
 cudaError_t launch_speakers(const DevDomain* doms, const int* x0, const int* y0, int n_dom, const DevSpeaker* spk,
                             int n_spk, float dx, float bw, float* set, float* fixed, float* p0, cudaStream_t st);
 cudaError_t launch_receivers(const DevReceiver* rec, int n_rec, const DevDomain* doms, const float* set, float* ring,

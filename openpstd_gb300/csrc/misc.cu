@@ -27,32 +27,42 @@ int stage_variants(int L, const StageVariant** out) {
 // (the reference does not recompute p0 after it), then px *= ax, py *= ay.
 // vx and vy of non-rigid domains were attenuated in the stage epilogue; rigid
 // domains (fields in the fixed buffer) get all four multiplies here.
-__global__ void pml_post_kernel(const int* idx, const DevDomain* doms, float* set, float* fixed, float* p0,
-                                const float* __restrict__ att) {
-    // rows over blockIdx.x (grid stride), columns over the threads: no division
-    const DevDomain d = doms[idx[blockIdx.y]];
-    float* base = d.fixed ? fixed : set;
-    for (int r = blockIdx.x; r < d.ny; r += gridDim.x) {
-        const float ay = d.att_yp >= 0 ? att[d.att_yp + r] : 1.f;
-        for (int i = threadIdx.x; i < d.nx; i += blockDim.x) {
-            const long long e = (long long)r * d.pitch_p + i;
-            const float px = base[d.o_px + e], py = base[d.o_py + e];
-            p0[d.o_p0 + e] = __fadd_rn(px, py);
-            if (d.att_xp >= 0) base[d.o_px + e] = __fmul_rn(px, att[d.att_xp + i]);
-            if (d.att_yp >= 0) base[d.o_py + e] = __fmul_rn(py, ay);
+__global__ void pml_post_kernel(const int* idx, int n, const int* off, const DevDomain* doms, float* set,
+                                float* fixed, float* p0, const float* __restrict__ att) {
+    // one element per thread, one block per (row, 128-column chunk) of a domain.
+    // off (prefix sums of the domains' block counts): a flat grid, the block's
+    // domain found by binary search; off == nullptr: domain = blockIdx.y.
+    int dj = blockIdx.y, lb = blockIdx.x;
+    if (off) {
+        int lo = 0, hi = n - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (off[mid] <= (int)blockIdx.x) lo = mid;
+            else hi = mid - 1;
         }
+        dj = lo;
+        lb = blockIdx.x - off[lo];
+    }
+    const DevDomain d = doms[idx[dj]];
+    float* base = d.fixed ? fixed : set;
+    const int chunks = (d.nx + 1 + 127) >> 7;   // vx rows have nx + 1 columns
+    const int r = lb / chunks, i = ((lb - r * chunks) << 7) + threadIdx.x;
+    if (r < d.ny && i < d.nx) {
+        const long long e = (long long)r * d.pitch_p + i;
+        const float px = base[d.o_px + e], py = base[d.o_py + e];
+        p0[d.o_p0 + e] = __fadd_rn(px, py);
+        if (d.att_xp >= 0) base[d.o_px + e] = __fmul_rn(px, att[d.att_xp + i]);
+        if (d.att_yp >= 0) base[d.o_py + e] = __fmul_rn(py, att[d.att_yp + r]);
     }
     if (d.fixed) {
-        for (int r = blockIdx.x; r < d.ny; r += gridDim.x)
-            for (int i = threadIdx.x; i < d.nx + 1; i += blockDim.x) {
-                const long long e = d.o_vx + (long long)r * d.pitch_vx + i;
-                if (d.att_xv >= 0) base[e] = __fmul_rn(base[e], att[d.att_xv + i]);
-            }
-        for (int r = blockIdx.x; r < d.ny + 1; r += gridDim.x)
-            for (int i = threadIdx.x; i < d.nx; i += blockDim.x) {
-                const long long e = d.o_vy + (long long)r * d.pitch_vy + i;
-                if (d.att_yv >= 0) base[e] = __fmul_rn(base[e], att[d.att_yv + r]);
-            }
+        if (r < d.ny && i < d.nx + 1 && d.att_xv >= 0) {
+            const long long e = d.o_vx + (long long)r * d.pitch_vx + i;
+            base[e] = __fmul_rn(base[e], att[d.att_xv + i]);
+        }
+        if (r < d.ny + 1 && i < d.nx && d.att_yv >= 0) {
+            const long long e = d.o_vy + (long long)r * d.pitch_vy + i;
+            base[e] = __fmul_rn(base[e], att[d.att_yv + r]);
+        }
     }
 }
 
@@ -131,10 +141,11 @@ __global__ void frame_kernel(const int* idx, const long long* dst_off, const Dev
         }
 }
 
-cudaError_t launch_pml_post(const int* idx, int n, const DevDomain* doms, float* set, float* fixed, float* p0,
-                            const float* att, cudaStream_t st) {
-    if (n <= 0) return cudaSuccess;
-    pml_post_kernel<<<dim3(128, n), 128, 0, st>>>(idx, doms, set, fixed, p0, att);
+cudaError_t launch_pml_post(const int* idx, int n, int blocks, const DevDomain* doms, float* set, float* fixed,
+                            float* p0, const float* att, cudaStream_t st, const int* off) {
+    if (n <= 0 || blocks <= 0) return cudaSuccess;
+    const dim3 grid = off ? dim3(blocks, 1) : dim3(blocks, n);
+    pml_post_kernel<<<grid, 128, 0, st>>>(idx, n, off, doms, set, fixed, p0, att);
     return cudaGetLastError();
 }
 

@@ -293,6 +293,7 @@ struct Server {
         K.ddoms.upload(hd);
         K.n_pml = (int)pml.size();
         K.dpml.upload(pml);
+        K.set_pml_blocks(pml);
         K.n_rec = (int)rec.size();
         drec.upload(rec);
         dslots.upload(slots);

@@ -623,6 +623,9 @@ static int solve_noalloc(const pstd_config* config, int n_steps, float* frame_de
         jobs.insert(jobs.end(), js.begin(), js.end());
     }
 
+    int pml_blocks = 1;   // one block per (row, 128-column chunk) of the largest PML domain
+    for (int k : pml_idx) pml_blocks = std::max(pml_blocks, (hd[k].ny + 1) * ((hd[k].nx + 1 + 127) >> 7));
+
     std::vector<DevReceiver> rec;
     for (auto& r : sc.receivers) rec.push_back({r.dom, r.row, r.col});
     std::vector<DevSpeaker> spk;
@@ -725,8 +728,8 @@ static int solve_noalloc(const pstd_config* config, int n_steps, float* frame_de
             }
         }
         if (!pml_idx.empty())
-            CK(launch_pml_post(reinterpret_cast<const int*>(base + o_pml), (int)pml_idx.size(), doms, F(o_set[B]),
-                               F(o_fixed), F(o_p0), F(o_att), st));
+            CK(launch_pml_post(reinterpret_cast<const int*>(base + o_pml), (int)pml_idx.size(), pml_blocks, doms,
+                               F(o_set[B]), F(o_fixed), F(o_p0), F(o_att), st));
         CK(cudaMemsetAsync(first_step, 0, sizeof(int), st));
         if (rec_dev && n_rec > 0)
             CK(launch_receivers(reinterpret_cast<const DevReceiver*>(base + o_rec), n_rec, doms, F(o_set[B]), rec_dev,
