@@ -271,3 +271,30 @@ def test_merged_launch(oracle_mod, monkeypatch):
     k.close()
     check_parity(oracle_mod, conf, 60, threads=16)
     check_parity(oracle_mod, scenes.rect(4, nx=1200, ny=90, steps=30), 30, threads=16)   # 2048, 256, 128
+
+
+def test_plan_cache_and_pinning(monkeypatch):
+    """A scene created a second time takes its autotuned plan from the
+    per-process cache (same variants, no timing); PSTD_PLAN pins one
+    variant per strip length; both give the oracle-checked results of the
+    variants they name (bit-identical to a solo run of those variants)."""
+    from openpstd_gb300 import scenes
+    from openpstd_gb300.kernel import PSTDKernel
+    monkeypatch.delenv("PSTD_VARIANT", raising=False)
+    conf = scenes.plain_square(8, n=150, steps=20)
+    a = PSTDKernel()
+    a.initialize_kernel(conf)
+    first = a.plan_info()
+    a.advance(20)
+    a.synchronize()
+    b = PSTDKernel()
+    b.initialize_kernel(conf)
+    assert "(plan cache)" in b.plan_info() and "(plan cache)" not in first
+    b.advance(20)
+    b.synchronize()
+    assert np.array_equal(a.receivers(), b.receivers())
+    monkeypatch.setenv("PSTD_PLAN", "128:1,256:0")
+    c = PSTDKernel()
+    c.initialize_kernel(conf)
+    info = c.plan_info()
+    assert info.count("pinned by PSTD_PLAN") == 2 and "(plan cache)" not in info
