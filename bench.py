@@ -69,6 +69,20 @@ def workload(name: str, seed: int):
     raise SystemExit(f"unknown workload {name}")
 
 
+def replica_totals(ms: float, cells: float, dist, device: str = "cuda"):
+    """Whole-job numbers of a replicas run: the slowest rank's time and the
+    cells of all ranks (every rank solves its own scene; no data-path
+    collective)."""
+    if dist is None:
+        return ms, float(cells)
+    import torch
+    t = torch.tensor([ms], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    c = torch.tensor([float(cells)], device=device, dtype=torch.float64)
+    dist.all_reduce(c)
+    return float(t.item()), float(c.item())
+
+
 def dist_setup():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     if ws <= 1:
@@ -301,7 +315,9 @@ def run_serve(args):
 
 
 def run_reference(args):
-    rank, ws, dist = dist_setup()
+    # the reference's CPU path runs once, on rank 0; other ranks leave at once
+    # (no process group: nothing is exchanged)
+    rank, ws = int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1"))
     if rank != 0:
         return
     from oracle import oracle
@@ -370,15 +386,7 @@ def run_ours(args):
     barrier()
     ms = e0.elapsed_time(e1)
     clocks = clk.summary()
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-        c = torch.tensor([float(cells)], device="cuda")
-        dist.all_reduce(c)
-        total_cells = float(c.item())
-    else:
-        total_cells = float(cells)
+    ms, total_cells = replica_totals(ms, cells, dist)
     value = total_cells * args.steps / (ms / 1e3) / 1e9
 
     # ---- pass-kernel timing (events around every pass launch)
@@ -424,10 +432,7 @@ def run_ours(args):
     e2e_s = time.perf_counter() - t0
     cfg_bytes = sum(ctypes.sizeof(x) for x in (ke._cc.c,)) + 40 * len(ce.Domains) + 12 * (len(ce.Speakers) + len(ce.Receivers))
     ke.close()
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s, _ = replica_totals(e2e_s, 0.0, dist)
     e2e = {"value": total_cells * e2e_steps / e2e_s / 1e9, "unit": METRIC,
            "h2d_bytes_per_step": cfg_bytes / e2e_steps,
            "d2h_bytes_per_step": (sizes["frame_bytes"] + sizes["sample_bytes"]) / e2e_steps,
