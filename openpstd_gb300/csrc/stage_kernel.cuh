@@ -727,6 +727,25 @@ __device__ __forceinline__ void gather_k(float2* sm, const StageArgs& A, const D
     if (!ydir) {
         // row pairs (2cs, 2cs+1), 16-byte loads, four chunks per lane in flight
         const int chunks = (n + 3) >> 2;
+        if (WPP == 1 && chunks <= 16) {
+            // short rows (the PML-normal strips): a half-warp per row pair
+            const int l16 = lane & 15, i = l16 << 2;
+#pragma unroll 2
+            for (int cs = 2 * warp + (lane >> 4); cs < CS; cs += 2 * NW) {
+                if (l16 >= chunks) continue;
+                const int s0 = 2 * cs;
+                const float* a0 = S.a + (long long)(job.first + s0) * S.pitch;
+                const float* b0 = TWO ? S.b + (long long)(job.first + s0) * S.pitch : nullptr;
+                float4 u = make_float4(0.f, 0.f, 0.f, 0.f), v = u;
+                if (s0 < count) u = TWO ? add4(ldf4(a0 + i), ldf4(b0 + i)) : ldf4(a0 + i);
+                if (s0 + 1 < count) v = TWO ? add4(ldf4(a0 + S.pitch + i), ldf4(b0 + S.pitch + i)) : ldf4(a0 + S.pitch + i);
+                float2* d = sm + cs * SP + W + i;
+                d[0] = make_float2(u.x, v.x);
+                if (i + 1 < n) d[1] = make_float2(u.y, v.y);
+                if (i + 2 < n) d[2] = make_float2(u.z, v.z);
+                if (i + 3 < n) d[3] = make_float2(u.w, v.w);
+            }
+        } else
         for (int cs = warp / WPP; cs < CS; cs += PST) {
             const int s0 = 2 * cs;
             const float* a0 = S.a + (long long)(job.first + s0) * S.pitch;
@@ -927,6 +946,41 @@ __device__ __forceinline__ void epilogue_k(const float2* sm, const StageArgs& A,
     if (!ydir) {
         // rows: four consecutive outputs per lane (16-byte loads / stores), two chunks in flight
         const int chunks = (nout + 3) >> 2;
+        if (WPP == 1 && chunks <= 16) {
+            // short rows (the PML-normal strips): a half-warp per row pair
+            const int l16 = lane & 15, i = l16 << 2;
+#pragma unroll 2
+            for (int cs = 2 * warp + (lane >> 4); cs < CS; cs += 2 * NW) {
+                if (l16 >= chunks || 2 * cs >= count) continue;
+                const long long r0 = fo + (long long)(job.first + 2 * cs) * fp;
+                const bool h1 = 2 * cs + 1 < count;
+                const float4 p0v = ldf4(prev + r0 + i);   // whole quads: rows are padded
+                const float4 p1v = h1 ? ldf4(prev + r0 + fp + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+                const float2* srow = sm + cs * SP + W;
+                float2 d[4];
+#pragma unroll
+                for (int e = 0; e < 4; e++) d[e] = (i + e < nout) ? srow[i + e] : make_float2(0.f, 0.f);
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    if (h == 1 && !h1) break;
+                    const float4 pv = h ? p1v : p0v;
+                    float v[4] = {pv.x, pv.y, pv.z, pv.w};
+#pragma unroll
+                    for (int e = 0; e < 4; e++) {
+                        v[e] = rk_update(v[e], h ? d[e].y : d[e].x, vel, cdt, rho, c2, rinv);
+                        if (att && i + e < nout) v[e] = __fmul_rn(v[e], A.att[ao + i + e]);
+                    }
+                    float* o = out + r0 + (h ? fp : 0) + i;
+                    if (i + 4 <= nout) {
+                        *reinterpret_cast<float4*>(o) = make_float4(v[0], v[1], v[2], v[3]);
+                    } else {
+#pragma unroll
+                        for (int e = 0; e < 4; e++)
+                            if (i + e < nout) o[e] = v[e];
+                    }
+                }
+            }
+        } else
         for (int cs = warp / WPP; cs < CS; cs += PST) {
             const float2* srow = sm + cs * SP + W;
             const long long r0 = fo + (long long)(job.first + 2 * cs) * fp;
