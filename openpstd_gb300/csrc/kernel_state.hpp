@@ -214,7 +214,6 @@ struct Kernel {
     size_t frame_floats = 0;
     DevBuf<int> dframe_doms;
     DevBuf<long long> dframe_off;
-    DevBuf<float> dframe;
 
     cudaGraphExec_t graphs[3] = {nullptr, nullptr, nullptr};
     bool graphs_ok = false;
@@ -562,7 +561,6 @@ struct Kernel {
         }
         dframe_doms.upload(frame_doms);
         dframe_off.upload(frame_off);
-        dframe.alloc(std::max<size_t>(frame_floats, 1));
 
         // ---- tables and the job plan (autotuned, or from the plan cache), then the launch form
         for (size_t i = 0; i < buckets.size(); i++) {

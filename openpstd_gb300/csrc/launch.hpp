@@ -65,8 +65,10 @@ cudaError_t launch_receivers(const DevReceiver* rec, int n_rec, const DevDomain*
 cudaError_t launch_server_receivers(const DevSrvReceiver* rec, int n_rec, const DevDomain* doms, const float* set,
                                     float* aux, int* scene_step, const int* slots, int n_slots, cudaStream_t st);
 // dense p0 = px + py of the given domains into dst (frames); sub > 1 keeps
-// every sub-th row and column (ceil(nx/sub) x ceil(ny/sub) values per domain)
+// every sub-th row and column (ceil(nx/sub) x ceil(ny/sub) values per domain);
+// n_rec floats of rec_src (a receiver row) are copied to rec_dst on the way
 cudaError_t launch_frame(const int* doms_idx, const long long* dst_off, int n, const DevDomain* doms, const float* set,
-                         float* dst, cudaStream_t st, int sub = 1);
+                         float* dst, cudaStream_t st, int sub = 1, const float* rec_src = nullptr, int n_rec = 0,
+                         float* rec_dst = nullptr);
 
 }  // namespace pstd

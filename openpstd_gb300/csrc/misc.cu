@@ -129,8 +129,12 @@ __global__ void server_receiver_kernel(const DevSrvReceiver* rec, int n_rec, con
 }
 
 // p0 = px + py of every `sub`-th row and column (sub = 1: the whole domain)
-__global__ void frame_kernel(const int* idx, const long long* dst_off, const DevDomain* doms,
-                             const float* __restrict__ set, float* dst, int sub) {
+__global__ void frame_kernel(const int* idx, const long long* dst_off, int n, const DevDomain* doms,
+                             const float* __restrict__ set, float* dst, int sub, const float* rec_src, int n_rec,
+                             float* rec_dst) {
+    if (blockIdx.x == 0 && blockIdx.y == 0)   // the step's receiver row rides along
+        for (int i = threadIdx.x; i < n_rec; i += blockDim.x) rec_dst[i] = rec_src[i];
+    if ((int)blockIdx.y >= n) return;
     const DevDomain d = doms[idx[blockIdx.y]];
     float* out = dst + dst_off[blockIdx.y];
     const int mx = (d.nx + sub - 1) / sub, my = (d.ny + sub - 1) / sub;
@@ -170,9 +174,10 @@ cudaError_t launch_server_receivers(const DevSrvReceiver* rec, int n_rec, const 
 }
 
 cudaError_t launch_frame(const int* idx, const long long* dst_off, int n, const DevDomain* doms, const float* set,
-                         float* dst, cudaStream_t st, int sub) {
-    if (n <= 0) return cudaSuccess;
-    frame_kernel<<<dim3(128, n), 128, 0, st>>>(idx, dst_off, doms, set, dst, sub);
+                         float* dst, cudaStream_t st, int sub, const float* rec_src, int n_rec, float* rec_dst) {
+    if (n <= 0 && n_rec <= 0) return cudaSuccess;
+    frame_kernel<<<dim3(256, std::max(n, 1)), 256, 0, st>>>(idx, dst_off, n, doms, set, dst, sub, rec_src, n_rec,
+                                                           rec_dst);
     return cudaGetLastError();
 }
 

@@ -62,12 +62,37 @@ static int run_frames(Kernel* k, const pstd_callbacks* cb, int save_nth = 0, int
     DevBuf<long long> dsub_off;
     if (sub > 1) dsub_off.upload(foff);
     const long long* doff = sub > 1 ? dsub_off.p : k->dframe_off.p;
-    const int K = 3;   // frames in flight
+    // Frames in flight.  A frame (and the step's receiver row) is formed on
+    // the compute stream into its own device slot and copied to pinned host
+    // memory on a copy stream, so the next steps do not queue behind the
+    // copy.  A slot is refilled only after the host has delivered its
+    // previous frame (the loop below waits for that), so neither the device
+    // nor the host slot is overwritten while a copy reads it.
+    const int K = 3;
     const size_t slot = frame_floats + (size_t)std::max(k->n_rec, 1);
+    const size_t slot_bytes = (frame_floats + (size_t)k->n_rec) * sizeof(float);
     PinnedBuf stage;
     stage.alloc(slot * K);
-    std::vector<cudaEvent_t> ev(K);
-    for (auto& e : ev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    DevBuf<float> dslots;
+    dslots.alloc(slot * K);
+    struct Sync {   // events and the copy stream, released on every exit
+        std::vector<cudaEvent_t> ready, done;
+        cudaStream_t copy = nullptr;
+        ~Sync() {
+            if (copy) cudaStreamSynchronize(copy), cudaStreamDestroy(copy);
+            for (auto e : ready) cudaEventDestroy(e);
+            for (auto e : done) cudaEventDestroy(e);
+        }
+    } sy;
+    for (int i = 0; i < K; i++) {
+        cudaEvent_t a, b;
+        CK(cudaEventCreateWithFlags(&a, cudaEventDisableTiming));
+        sy.ready.push_back(a);
+        CK(cudaEventCreateWithFlags(&b, cudaEventDisableTiming));
+        sy.done.push_back(b);
+    }
+    CK(cudaStreamCreateWithFlags(&sy.copy, cudaStreamNonBlocking));
+    auto& ev = sy.done;
     struct Pending { int frame, slot; };
     std::deque<Pending> q;
     int status = PSTD_OK;
@@ -98,17 +123,15 @@ static int run_frames(Kernel* k, const pstd_callbacks* cb, int save_nth = 0, int
             int s = next_slot;
             next_slot = (next_slot + 1) % K;
             float* base = stage.p + slot * s;
-            if (frame_floats) {
-                CK(launch_frame(k->dframe_doms.p, doff, (int)k->frame_doms.size(), k->ddoms.p, k->sets[k->cur].p,
-                                k->dframe.p, k->stream, sub));
-                CK(cudaMemcpyAsync(base, k->dframe.p, frame_floats * sizeof(float), cudaMemcpyDeviceToHost, k->stream));
-            }
-            if (k->n_rec > 0) {
-                int row = (k->steps - 1) % k->ring_cap;
-                CK(cudaMemcpyAsync(base + frame_floats, k->dring.p + (size_t)row * k->n_rec, k->n_rec * sizeof(float),
-                                   cudaMemcpyDeviceToHost, k->stream));
-            }
-            CK(cudaEventRecord(ev[s], k->stream));
+            float* dbase = dslots.p + slot * s;
+            const int row = (k->steps - 1) % k->ring_cap;
+            CK(launch_frame(k->dframe_doms.p, doff, frame_floats ? (int)k->frame_doms.size() : 0, k->ddoms.p,
+                            k->sets[k->cur].p, dbase, k->stream, sub, k->dring.p + (size_t)row * k->n_rec, k->n_rec,
+                            dbase + frame_floats));
+            CK(cudaEventRecord(sy.ready[s], k->stream));
+            CK(cudaStreamWaitEvent(sy.copy, sy.ready[s], 0));
+            if (slot_bytes) CK(cudaMemcpyAsync(base, dbase, slot_bytes, cudaMemcpyDeviceToHost, sy.copy));
+            CK(cudaEventRecord(ev[s], sy.copy));
             q.push_back({f, s});
         } else {
             log(PSTD_LOG_INFO, "Finished frame: " + std::to_string(f));
@@ -120,7 +143,7 @@ static int run_frames(Kernel* k, const pstd_callbacks* cb, int save_nth = 0, int
         q.pop_front();
     }
     CK(cudaStreamSynchronize(k->stream));
-    for (auto& e : ev) cudaEventDestroy(e);
+    CK(cudaStreamSynchronize(sy.copy));
     if (status == PSTD_OK) log(PSTD_LOG_INFO, "Succesfully finished simulation");
     else g_error = "a callback asked to stop the run";
     return status;

@@ -21,6 +21,7 @@ Frames are numpy float32 arrays of length Nx*Ny, row-major with x fastest
 from __future__ import annotations
 
 import ctypes
+import os
 from typing import List, Optional
 
 import numpy as np
@@ -88,6 +89,32 @@ def _log_bridge(target: Optional[KernelCallbackLog]):
     return _lib.LOG(_log)
 
 
+_COPY_CHUNK = 1 << 18            # floats per copy task (1 MiB)
+_COPY_THREADS = 8
+_copy_pool = None
+
+
+def _copy_frame(ptr, n: int) -> np.ndarray:
+    """A float32 array the callee owns, copied from the library's staging
+    buffer (valid only during the callback).  Large frames are copied in
+    1 MiB chunks by a small thread pool (numpy releases the GIL while it
+    copies): one host thread moves about 50 GB/s, less than a frame stream
+    of a large scene needs."""
+    src = np.ctypeslib.as_array(ptr, shape=(n,))
+    if n < 2 * _COPY_CHUNK:
+        return src.copy()
+    global _copy_pool
+    if _copy_pool is None:
+        from concurrent.futures import ThreadPoolExecutor
+        _copy_pool = ThreadPoolExecutor(min(_COPY_THREADS, os.cpu_count() or 1), thread_name_prefix="pstd-frame")
+    dst = np.empty(n, np.float32)
+    parts = min(_COPY_THREADS, -(-n // _COPY_CHUNK))
+    step = -(-n // parts)
+    list(_copy_pool.map(lambda i: np.copyto(dst[i * step:(i + 1) * step], src[i * step:(i + 1) * step]),
+                        range(parts)))
+    return dst
+
+
 class PSTDKernel(KernelInterface):
     """GPU solver behind the reference's PSTDKernel interface.
 
@@ -129,7 +156,7 @@ class PSTDKernel(KernelInterface):
 
         def _frame(user, frame, domain, data, n):
             try:
-                callback.WriteFrame(int(frame), int(domain), np.ctypeslib.as_array(data, shape=(n,)).copy())
+                callback.WriteFrame(int(frame), int(domain), _copy_frame(data, n))
                 return 0
             except Exception as e:   # stop the run, re-raise after it returns
                 errors.append(e)
