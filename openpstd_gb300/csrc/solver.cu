@@ -68,9 +68,11 @@ static int run_frames(Kernel* k, const pstd_callbacks* cb, int save_nth = 0, int
     // copy.  A slot is refilled only after the host has delivered its
     // previous frame (the loop below waits for that), so neither the device
     // nor the host slot is overwritten while a copy reads it.
-    const int K = 3;
+    // Small frames get more slots (up to 8, within 64 MiB) so that the
+    // device runs further ahead of a host whose callbacks take uneven time.
     const size_t slot = frame_floats + (size_t)std::max(k->n_rec, 1);
     const size_t slot_bytes = (frame_floats + (size_t)k->n_rec) * sizeof(float);
+    const int K = (int)std::min<size_t>(8, std::max<size_t>(3, (size_t(64) << 20) / (slot * sizeof(float))));
     PinnedBuf stage;
     stage.alloc(slot * K);
     DevBuf<float> dslots;
