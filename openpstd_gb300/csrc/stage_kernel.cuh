@@ -554,9 +554,20 @@ __device__ __forceinline__ void mid_pass(float2* sm, const float2* filt, int tid
     for (int it = tid; it < ITEMS; it += NTH) {
         const int cs = it % C::CS, blk = it / C::CS;
         float2* base = sm + cs * C::SP + blk * R;
+        // Register q holds position (q + rot) mod R of the block.  A circular
+        // shift of the input multiplies the spectrum by a phase only; the
+        // filter leaves it and the inverse DFT turns it back into the same
+        // shift, so register q is stored back where it came from.  Blocks lie
+        // a multiple of 16 float2 apart (one bank set) and a half-warp holds
+        // only CS strips: rotating by the block index spreads its accesses
+        // over all banks (4-way conflicts at CS = 4 without it).  Radix 32
+        // keeps the natural order (32 rotated addresses cost registers), and
+        // so do jobs of 8 or more strips: at most 2-way conflicts there, less
+        // than the address arithmetic costs.
+        const int rot = (R <= 16 && C::CS <= 4) ? (blk & (R - 1)) : 0;
         float2 x[R];
 #pragma unroll
-        for (int q = 0; q < R; q++) x[q] = base[q];
+        for (int q = 0; q < R; q++) x[q] = base[(q + rot) & (R - 1)];
         DFT<R, false>::run(x);
 #pragma unroll
         for (int h = 0; h < R / 2; h++) {
@@ -566,7 +577,7 @@ __device__ __forceinline__ void mid_pass(float2* sm, const float2* filt, int tid
         }
         DFT<R, true>::run(x);
 #pragma unroll
-        for (int q = 0; q < R; q++) base[q] = x[q];
+        for (int q = 0; q < R; q++) base[(q + rot) & (R - 1)] = x[q];
     }
 }
 
