@@ -45,7 +45,7 @@ __device__ __noinline__ void merged_job(float2* sm, const StageArgs& A, int j, i
 
 // (the arguments stay in parameter space: the job functions read them by address)
 __global__ void __launch_bounds__(MERGED_NT, 3) stage_all(const __grid_constant__ StageArgs A, int n_jobs, int* counter) {
-    extern __shared__ float2 sm[];
+    extern __shared__ __align__(16) float2 sm[];
     __shared__ int s_job;
     const int tid = threadIdx.x;
     for (;;) {

@@ -543,6 +543,15 @@ __device__ __forceinline__ void inv_pass(float2* sm, const float2* tw, int tid, 
     }
 }
 
+// Rotation mask of the mid pass (see mid_pass): jobs of at most 4 strips with
+// radix 4..16 (radix 32 would hold 16 rotated addresses); 16-byte accesses
+// need an even strip pitch, which CS <= 4 gives (pad 16 / CS).
+template <class C, int R>
+__host__ __device__ constexpr int mid_rot_mask() {
+    if (R < 4 || R > 16 || C::CS > 4 || (C::SP & 1)) return 0;
+    return (8 / C::CS < R / 2 ? 8 / C::CS : R / 2) - 1;
+}
+
 // last forward pass (blocks of R contiguous positions), filter, first inverse pass
 template <class C, int R, int NTH, bool SMT>
 __device__ __forceinline__ void mid_pass(float2* sm, const float2* filt, int tid) {
@@ -554,20 +563,27 @@ __device__ __forceinline__ void mid_pass(float2* sm, const float2* filt, int tid
     for (int it = tid; it < ITEMS; it += NTH) {
         const int cs = it % C::CS, blk = it / C::CS;
         float2* base = sm + cs * C::SP + blk * R;
-        // Register q holds position (q + rot) mod R of the block.  A circular
-        // shift of the input multiplies the spectrum by a phase only; the
-        // filter leaves it and the inverse DFT turns it back into the same
-        // shift, so register q is stored back where it came from.  Blocks lie
-        // a multiple of 16 float2 apart (one bank set) and a half-warp holds
-        // only CS strips: rotating by the block index spreads its accesses
-        // over all banks (4-way conflicts at CS = 4 without it).  Radix 32
-        // keeps the natural order (32 rotated addresses cost registers), and
-        // so do jobs of 8 or more strips: at most 2-way conflicts there, less
-        // than the address arithmetic costs.
-        const int rot = (R <= 16 && C::CS <= 4) ? (blk & (R - 1)) : 0;
+        // Registers 2h, 2h + 1 hold positions (2h + rot) mod R and the one
+        // after it.  A circular shift of the input multiplies the spectrum by
+        // a phase only; the filter leaves it and the inverse DFT turns it back
+        // into the same shift, so each register is stored back where it came
+        // from.  Blocks lie a multiple of 8 float2 apart and a quarter-warp
+        // holds only CS strips, so without the shift its 16-byte accesses
+        // meet in the same banks (2-way at CS = 4, 4-way at CS = 2).
+        constexpr int RM = mid_rot_mask<C, R>();
+        const int rot = 2 * (blk & RM);
         float2 x[R];
+        if constexpr (RM == 0) {
 #pragma unroll
-        for (int q = 0; q < R; q++) x[q] = base[(q + rot) & (R - 1)];
+            for (int q = 0; q < R; q++) x[q] = base[q];
+        } else {
+#pragma unroll
+            for (int h = 0; h < R / 2; h++) {
+                const float4 v = *reinterpret_cast<const float4*>(base + ((2 * h + rot) & (R - 1)));
+                x[2 * h] = make_float2(v.x, v.y);
+                x[2 * h + 1] = make_float2(v.z, v.w);
+            }
+        }
         DFT<R, false>::run(x);
 #pragma unroll
         for (int h = 0; h < R / 2; h++) {
@@ -576,8 +592,15 @@ __device__ __forceinline__ void mid_pass(float2* sm, const float2* filt, int tid
             x[2 * h + 1] = cmul(x[2 * h + 1], make_float2(v.z, v.w));
         }
         DFT<R, true>::run(x);
+        if constexpr (RM == 0) {
 #pragma unroll
-        for (int q = 0; q < R; q++) base[(q + rot) & (R - 1)] = x[q];
+            for (int q = 0; q < R; q++) base[q] = x[q];
+        } else {
+#pragma unroll
+            for (int h = 0; h < R / 2; h++)
+                *reinterpret_cast<float4*>(base + ((2 * h + rot) & (R - 1))) =
+                    make_float4(x[2 * h].x, x[2 * h].y, x[2 * h + 1].x, x[2 * h + 1].y);
+        }
     }
 }
 
@@ -1107,7 +1130,7 @@ __device__ __forceinline__ void epilogue(const float2* sm, const StageArgs& A, c
 // ---------------------------------------------------------------- plain form
 template <class C>
 __global__ void __launch_bounds__(C::NT, C::MINB) stage_kernel(StageArgs A) {
-    extern __shared__ float2 sm[];
+    extern __shared__ __align__(16) float2 sm[];
     const DevJob job = A.jobs[blockIdx.x];
     const DevDomain dom = A.doms[job.dom];
     if (job.kind & JK_COPY) {
@@ -1132,7 +1155,7 @@ __global__ void __launch_bounds__(C::NT, C::MINB) stage_kernel(StageArgs A) {
 template <class C>
 __global__ void __launch_bounds__(C::NT + C::NTP, 1) stage_ws(StageArgs A, int n_jobs) {
     constexpr int NTC = C::NT, NTP = C::NTP, ALL = C::NT + C::NTP;
-    extern __shared__ float2 sm[];
+    extern __shared__ __align__(16) float2 sm[];
     float2* tws = sm + 2 * C::BUF;
     float2* flt = tws + C::TWN;
     const int tid = threadIdx.x;
@@ -1440,7 +1463,7 @@ __device__ __forceinline__ void pipe_epilogue(const float2* sm, const float* sp,
 template <class C>
 __global__ void __launch_bounds__(C::NT, C::MINB) stage_pipe(StageArgs A, int n_jobs) {
     constexpr int NT = C::NT, S2 = 2 * C::CS;
-    extern __shared__ float2 sm[];
+    extern __shared__ __align__(16) float2 sm[];
     const int rc = A.row_cap;
     float* slots = reinterpret_cast<float*>(sm + C::BUF);
     const int slot_f = pipe_slot_floats(S2, rc);
@@ -1514,7 +1537,7 @@ __device__ __forceinline__ void stage_prev_in(float* sp, const StageArgs& A, con
 
 template <class C>
 __global__ void __launch_bounds__(C::NT, C::MINB) stage_sprev(StageArgs A) {
-    extern __shared__ float2 sm[];
+    extern __shared__ __align__(16) float2 sm[];
     constexpr int S2 = 2 * C::CS;
     const int rc = A.row_cap;
     float* sp = reinterpret_cast<float*>(sm + C::BUF);
