@@ -744,6 +744,21 @@ __device__ void copy_axis(const StageArgs& A, const DevDomain& D, bool ydir, int
 
 // ---- step 1: strips + bands + padding of one job into `sm` (NTH threads)
 // TWO: the strip's p0 is formed as px + py (else one field: velocity or stale p0)
+// Four positions of a row pair (strips 2cs, 2cs + 1 interleaved as one
+// complex strip) as two 16-byte shared accesses; d must be 16-byte aligned.
+__device__ __forceinline__ void store_pairs(float2* d, float4 u, float4 v) {
+    float4* d4 = reinterpret_cast<float4*>(d);
+    d4[0] = make_float4(u.x, v.x, u.y, v.y);
+    d4[1] = make_float4(u.z, v.z, u.w, v.w);
+}
+__device__ __forceinline__ void load_pairs(const float2* s, float2 (&d)[4]) {
+    const float4 a = reinterpret_cast<const float4*>(s)[0], b = reinterpret_cast<const float4*>(s)[1];
+    d[0] = make_float2(a.x, a.y);
+    d[1] = make_float2(a.z, a.w);
+    d[2] = make_float2(b.x, b.y);
+    d[3] = make_float2(b.z, b.w);
+}
+
 template <class C, int NTH, bool ZERO, bool TWO>
 __device__ __forceinline__ void gather_k(float2* sm, const StageArgs& A, const DevJob& job, const DevDomain& dom,
                                          bool first, const Src& S, int tid) {
@@ -761,6 +776,7 @@ __device__ __forceinline__ void gather_k(float2* sm, const StageArgs& A, const D
     if (!ydir) {
         // row pairs (2cs, 2cs+1), 16-byte loads, four chunks per lane in flight
         const int chunks = (n + 3) >> 2;
+        const bool pair16 = (SP % 2 == 0) && !(W & 1);   // 16-byte aligned pairs in shared memory
         if (WPP == 1 && chunks <= 16) {
             // short rows (the PML-normal strips): a half-warp per row pair
             const int l16 = lane & 15, i = l16 << 2;
@@ -774,10 +790,14 @@ __device__ __forceinline__ void gather_k(float2* sm, const StageArgs& A, const D
                 if (s0 < count) u = TWO ? add4(ldf4(a0 + i), ldf4(b0 + i)) : ldf4(a0 + i);
                 if (s0 + 1 < count) v = TWO ? add4(ldf4(a0 + S.pitch + i), ldf4(b0 + S.pitch + i)) : ldf4(a0 + S.pitch + i);
                 float2* d = sm + cs * SP + W + i;
-                d[0] = make_float2(u.x, v.x);
-                if (i + 1 < n) d[1] = make_float2(u.y, v.y);
-                if (i + 2 < n) d[2] = make_float2(u.z, v.z);
-                if (i + 3 < n) d[3] = make_float2(u.w, v.w);
+                if (pair16 && i + 4 <= n) {
+                    store_pairs(d, u, v);
+                } else {
+                    d[0] = make_float2(u.x, v.x);
+                    if (i + 1 < n) d[1] = make_float2(u.y, v.y);
+                    if (i + 2 < n) d[2] = make_float2(u.z, v.z);
+                    if (i + 3 < n) d[3] = make_float2(u.w, v.w);
+                }
             }
         } else
         for (int cs = warp / WPP; cs < CS; cs += PST) {
@@ -802,10 +822,14 @@ __device__ __forceinline__ void gather_k(float2* sm, const StageArgs& A, const D
                     const int c = c0 + q * WPP * 32, i = c << 2;
                     if (c < chunks) {
                         float2* d = sm + cs * SP + W + i;
-                        d[0] = make_float2(u[q].x, v[q].x);
-                        if (i + 1 < n) d[1] = make_float2(u[q].y, v[q].y);
-                        if (i + 2 < n) d[2] = make_float2(u[q].z, v[q].z);
-                        if (i + 3 < n) d[3] = make_float2(u[q].w, v[q].w);
+                        if (pair16 && i + 4 <= n) {
+                            store_pairs(d, u[q], v[q]);
+                        } else {
+                            d[0] = make_float2(u[q].x, v[q].x);
+                            if (i + 1 < n) d[1] = make_float2(u[q].y, v[q].y);
+                            if (i + 2 < n) d[2] = make_float2(u[q].z, v[q].z);
+                            if (i + 3 < n) d[3] = make_float2(u[q].w, v[q].w);
+                        }
                     }
                 }
             }
@@ -980,6 +1004,7 @@ __device__ __forceinline__ void epilogue_k(const float2* sm, const StageArgs& A,
     if (!ydir) {
         // rows: four consecutive outputs per lane (16-byte loads / stores), two chunks in flight
         const int chunks = (nout + 3) >> 2;
+        const bool pair16 = (SP % 2 == 0) && !(W & 1);   // 16-byte aligned pairs in shared memory
         if (WPP == 1 && chunks <= 16) {
             // short rows (the PML-normal strips): a half-warp per row pair
             const int l16 = lane & 15, i = l16 << 2;
@@ -992,8 +1017,12 @@ __device__ __forceinline__ void epilogue_k(const float2* sm, const StageArgs& A,
                 const float4 p1v = h1 ? ldf4(prev + r0 + fp + i) : make_float4(0.f, 0.f, 0.f, 0.f);
                 const float2* srow = sm + cs * SP + W;
                 float2 d[4];
+                if (pair16 && i + 4 <= nout) {
+                    load_pairs(srow + i, d);
+                } else {
 #pragma unroll
-                for (int e = 0; e < 4; e++) d[e] = (i + e < nout) ? srow[i + e] : make_float2(0.f, 0.f);
+                    for (int e = 0; e < 4; e++) d[e] = (i + e < nout) ? srow[i + e] : make_float2(0.f, 0.f);
+                }
 #pragma unroll
                 for (int h = 0; h < 2; h++) {
                     if (h == 1 && !h1) break;
@@ -1037,8 +1066,12 @@ __device__ __forceinline__ void epilogue_k(const float2* sm, const StageArgs& A,
                     const int i = (c0 + q * WPP * 32) << 2;
                     if (i >= nout) continue;
                     float2 d[4];
+                    if (pair16 && i + 4 <= nout) {
+                        load_pairs(srow + i, d);
+                    } else {
 #pragma unroll
-                    for (int e = 0; e < 4; e++) d[e] = (i + e < nout) ? srow[i + e] : make_float2(0.f, 0.f);
+                        for (int e = 0; e < 4; e++) d[e] = (i + e < nout) ? srow[i + e] : make_float2(0.f, 0.f);
+                    }
 #pragma unroll
                     for (int h = 0; h < 2; h++) {
                         if (h == 1 && !h1) break;
