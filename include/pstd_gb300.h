@@ -130,7 +130,10 @@ int pstd_get_metadata(pstd_kernel* k, int32_t* n_domains, int32_t* dims, int32_t
 /* Replaces PSTDKernel::run with the GPU solver (kernel/PSTDKernel.cpp:121-148,
  * kernel/Solver.cpp:62-93).  Runs Framecount time steps from the current
  * state, emitting frames and receiver samples through cb.  Blocks the
- * calling thread; callbacks run on it, in frame order. */
+ * calling thread; callbacks run on it, in frame order.  The device runs
+ * ahead of the callbacks by as many frames as fit in 64 MiB (at least 3, at
+ * most 8): each is copied to pinned host memory on a copy stream while later
+ * steps compute. */
 int pstd_run(pstd_kernel* k, const pstd_callbacks* cb);
 
 /* pstd_run with frame subsampling on the device (no reference counterpart):
