@@ -291,8 +291,11 @@ int pstd_server_stats(pstd_server* s, int64_t* stats);
  * process exits.  Scenes that need more are rejected with PSTD_ERR_INVALID
  * and a message giving the bytes needed (use pstd_create for those).
  * The first call on a device takes the array's device address
- * (cudaGetSymbolAddress) with that device current; make that first call
- * before any stream capture.  Every call shares the array and clears it
+ * (cudaGetSymbolAddress) with that device current and keeps it for the
+ * process; make that first call before any stream capture.  A
+ * cudaDeviceReset unloads the array with the module, so that address no
+ * longer holds: after a reset, do not call this entry point again in the
+ * same process.  Every call shares the array and clears it
  * itself; calls whose GPU work overlaps (other streams, other threads on one
  * device) race on it.  The plan upload is a pageable host-to-device copy,
  * so the call waits for work already queued on `stream`.  Each strip length

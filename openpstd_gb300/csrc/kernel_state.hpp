@@ -2,6 +2,8 @@
 // tables, device field layout, strip-job plan, CUDA graphs) shared by the C
 // ABI of solver.cu and the serving loop of server.cu.
 #pragma once
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -206,7 +208,7 @@ struct Kernel {
     std::vector<float2> filt;
     std::map<std::tuple<int, int, int, int, int, int, float>, int> filt_off;   // (L, vel, radices, dx)
     std::vector<float2> tw;
-    std::map<std::tuple<int, int, int, int, int>, int> tw_off;   // (L, radices)
+    std::map<std::tuple<int, int, int, int, int, int>, int> tw_off;   // (L, radices, lane-pair split)
 
     // frames
     std::vector<int> frame_doms;
@@ -214,6 +216,11 @@ struct Kernel {
     size_t frame_floats = 0;
     DevBuf<int> dframe_doms;
     DevBuf<long long> dframe_off;
+
+    // staged (TMA) form: a 2-D tensor map per (domain, field, state set) and
+    // the error word a CTA sets when a staged copy does not arrive in time
+    DevBuf<unsigned char> dmaps;
+    DevBuf<int> derr;
 
     cudaGraphExec_t graphs[3] = {nullptr, nullptr, nullptr};
     bool graphs_ok = false;
@@ -292,7 +299,7 @@ struct Kernel {
     // holds [n1][k] = exp(-2 pi i n1 k / M) for n1 < M/R, k < R; the offset
     // of every pass is a multiple of 2 float2 (16-byte loads)
     int twiddles_of(const StageVariant* v) {
-        auto key = std::make_tuple(v->L, v->r[0], v->r[1], v->r[2], v->r[3]);
+        auto key = std::make_tuple(v->L, v->r[0], v->r[1], v->r[2], v->r[3], v->shf);
         auto it = tw_off.find(key);
         if (it != tw_off.end()) return it->second;
         if (tw.size() & 1) tw.push_back(make_float2(0, 0));
@@ -306,6 +313,15 @@ struct Kernel {
                     tw.push_back(make_float2((float)std::cos(a), (float)std::sin(a)));
                 }
             M = Q;
+        }
+        if (v->shf) {
+            // last radix 2H over a lane pair: H ones (lane 0), then exp(-2 pi i j / 2H), j < H (lane 1)
+            const int H = M / 2;
+            for (int j = 0; j < H; j++) tw.push_back(make_float2(1.f, 0.f));
+            for (int j = 0; j < H; j++) {
+                double a = -2.0 * M_PI * (double)j / M;
+                tw.push_back(make_float2((float)std::cos(a), (float)std::sin(a)));
+            }
         }
         tw_off[key] = o;
         return o;
@@ -408,25 +424,25 @@ struct Kernel {
         for (auto& sc : scenes) framecount = std::max(framecount, sc.s.framecount());
     }
 
-    void build_device() {
-        if (const char* e = std::getenv("PSTD_AUTOTUNE")) autotune = std::atoi(e) != 0;
-        // PSTD_VARIANT=i pins every bucket to its i-th compiled variant (tests)
-        int forced = -1;
-        if (const char* e = std::getenv("PSTD_VARIANT")) { forced = std::atoi(e); autotune = false; }
-        CK(cudaGetDevice(&device));
-        CK(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
-        CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
-
-        // ---- layout
+    // Layout of every domain's fields in a state set, the fixed buffer and the
+    // p0 array (device.cuh: rows padded to 32 floats, each field starting on a
+    // 128-byte boundary), the PML attenuation profiles and the PML domains.
+    // pstd_create and the allocation-free solve both use it.
+    struct FieldLayout {
+        std::vector<DevDomain> doms;
+        std::vector<float> att;      // never empty
+        std::vector<int> pml_idx;
+        size_t set_floats = 0, fixed_floats = 0, p0_floats = 0;
+    };
+    FieldLayout layout_fields() const {
         auto round32 = [](long long v) { return (v + 31) / 32 * 32; };
         long long off = 0, foff = 0, poff = 0;
-        hdoms.resize(gdom.size());
-        std::vector<float> att;
-        std::vector<int> pml_idx;
+        FieldLayout out;
+        out.doms.resize(gdom.size());
         for (size_t k = 0; k < gdom.size(); k++) {
             const Domain& d = dom((int)k);
             const Scene& sc = scene_of((int)k);
-            DevDomain& h = hdoms[k];
+            DevDomain& h = out.doms[k];
             std::memset(&h, 0, sizeof h);
             h.nx = d.nx; h.ny = d.ny;
             h.pitch_p = (int)round32(d.nx);
@@ -442,33 +458,51 @@ struct Kernel {
             h.o_p0 = poff; poff = round32(poff + (long long)h.pitch_p * d.ny);
             h.rho = d.rho;
             h.c2 = sc.s.c1 * sc.s.c1;
-            float dt = sc.s.dt();
+            const float dt = sc.s.dt();
             for (int i = 0; i < 6; i++) h.cdt[i] = dt * sc.s.rk[i];
             h.pml = d.pml;
             h.att_xp = h.att_xv = h.att_yp = h.att_yv = -1;
             if (d.pml) {
-                pml_idx.push_back((int)k);
+                out.pml_idx.push_back((int)k);
                 std::vector<double> prof;
-                if (d.att_x) {
-                    pml_profile(sc.s, false, d.asc_x, prof);
-                    h.att_xp = (int)att.size(); for (double v : prof) att.push_back((float)v);
-                    pml_profile(sc.s, true, d.asc_x, prof);
-                    h.att_xv = (int)att.size(); for (double v : prof) att.push_back((float)v);
-                }
-                if (d.att_y) {
-                    pml_profile(sc.s, false, d.asc_y, prof);
-                    h.att_yp = (int)att.size(); for (double v : prof) att.push_back((float)v);
-                    pml_profile(sc.s, true, d.asc_y, prof);
-                    h.att_yv = (int)att.size(); for (double v : prof) att.push_back((float)v);
-                }
+                auto put = [&](bool vel, bool asc, int& at) {
+                    pml_profile(sc.s, vel, asc, prof);
+                    at = (int)out.att.size();
+                    for (double v : prof) out.att.push_back((float)v);
+                };
+                if (d.att_x) { put(false, d.asc_x, h.att_xp); put(true, d.asc_x, h.att_xv); }
+                if (d.att_y) { put(false, d.asc_y, h.att_yp); put(true, d.asc_y, h.att_yv); }
             }
+        }
+        out.set_floats = (size_t)std::max<long long>(off, 32);
+        out.fixed_floats = (size_t)std::max<long long>(foff, 32);
+        out.p0_floats = (size_t)std::max<long long>(poff, 32);
+        if (out.att.empty()) out.att.push_back(1.f);
+        return out;
+    }
+
+    void build_device() {
+        if (const char* e = std::getenv("PSTD_AUTOTUNE")) autotune = std::atoi(e) != 0;
+        // PSTD_VARIANT=i pins every bucket to its i-th compiled variant (tests)
+        int forced = -1;
+        if (const char* e = std::getenv("PSTD_VARIANT")) { forced = std::atoi(e); autotune = false; }
+        CK(cudaGetDevice(&device));
+        CK(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
+        CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+
+        // ---- layout
+        FieldLayout lay = layout_fields();
+        hdoms = lay.doms;
+        std::vector<float>& att = lay.att;
+        std::vector<int>& pml_idx = lay.pml_idx;
+        for (size_t k = 0; k < gdom.size(); k++) {
+            const Domain& d = dom((int)k);
             if (!d.rigid) cells += (int64_t)d.nx * d.ny;
             if (!d.pml) air_cells += (int64_t)d.nx * d.ny;
         }
-        set_floats = (size_t)std::max<long long>(off, 32);
-        fixed_floats = (size_t)std::max<long long>(foff, 32);
-        p0_floats = (size_t)std::max<long long>(poff, 32);
-        if (att.empty()) att.push_back(1.f);
+        set_floats = lay.set_floats;
+        fixed_floats = lay.fixed_floats;
+        p0_floats = lay.p0_floats;
         datt.upload(att);
         n_pml = (int)pml_idx.size();
         dpml.upload(pml_idx);
@@ -520,6 +554,9 @@ struct Kernel {
         p0.alloc(p0_floats);
         init_p0.alloc(p0_floats);
         first_step.alloc(scenes.size());
+        derr.alloc(1);
+        CK(cudaMemset(derr.p, 0, sizeof(int)));
+        build_tensor_maps();
         CK(cudaMemsetAsync(init_set.p, 0, set_floats * sizeof(float), stream));
         CK(cudaMemsetAsync(init_fixed.p, 0, fixed_floats * sizeof(float), stream));
         CK(cudaMemsetAsync(init_p0.p, 0, p0_floats * sizeof(float), stream));
@@ -636,7 +673,63 @@ struct Kernel {
         a.stage = k;
         a.last = k == 5;
         a.row_cap = rc;
+        a.maps = dmaps.p;
+        a.set_in = k == 0 ? c : ((k - 1) % 2 == 0 ? A : B);
+        a.set_prev = c;
+        a.err = derr.p;
         return a;
+    }
+
+    // Tensor maps of the staged form: for every non-rigid domain the 2-D
+    // [rows x columns] view of px, py, vx, vy in each state set and of its p0
+    // array, boxes of 4 columns x tma_box_rows(rows) rows (stage_tma.cuh).
+    // Needs the driver's cuTensorMapEncodeTiled; without it the staged
+    // variants are left out of the plan.
+    void build_tensor_maps() {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || !fn) {
+            cudaGetLastError();
+            return;
+        }
+        auto encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+        std::vector<unsigned char> maps((size_t)gdom.size() * 16 * PSTD_TMAP_BYTES, 0);
+        auto put = [&](size_t idx, const float* base, int cols, int rows, int pitch) {
+            CUtensorMap* m = reinterpret_cast<CUtensorMap*>(maps.data() + idx * PSTD_TMAP_BYTES);
+            const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+            const cuuint64_t strides[1] = {(cuuint64_t)pitch * sizeof(float)};
+            const cuuint32_t box[2] = {4, (cuuint32_t)tma_box_rows(rows)};
+            const cuuint32_t estr[2] = {1, 1};
+            const CUresult r = encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box,
+                                      estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+            if (r != CUDA_SUCCESS) throw CudaError("cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+        };
+        for (size_t d = 0; d < gdom.size(); d++) {
+            const DevDomain& h = hdoms[d];
+            if (h.fixed) continue;
+            for (int set = 0; set < 3; set++) {
+                const float* b = sets[set].p;
+                put((d * 4 + 0) * 4 + set, b + h.o_px, h.nx, h.ny, h.pitch_p);
+                put((d * 4 + 1) * 4 + set, b + h.o_py, h.nx, h.ny, h.pitch_p);
+                put((d * 4 + 2) * 4 + set, b + h.o_vx, h.nx + 1, h.ny, h.pitch_vx);
+                put((d * 4 + 3) * 4 + set, b + h.o_vy, h.nx, h.ny + 1, h.pitch_vy);
+            }
+            put((d * 4 + 0) * 4 + 3, p0.p + h.o_p0, h.nx, h.ny, h.pitch_p);
+        }
+        dmaps.upload(maps);
+    }
+
+    // a staged copy that did not arrive in time is reported once, here
+    void check_stage_error() {
+        if (!derr.p) return;
+        int e = 0;
+        CK(cudaMemcpy(&e, derr.p, sizeof e, cudaMemcpyDeviceToHost));
+        if (e) {
+            CK(cudaMemset(derr.p, 0, sizeof(int)));
+            throw CudaError("a staged (TMA) copy of the stage kernel did not complete in time");
+        }
     }
 
     void upload_tables() {
@@ -673,6 +766,7 @@ struct Kernel {
                     if (vs[i].persistent && !one_filter_pair(all[i], fpv[i], fvv[i])) all[i].clear();
                     if (vs[i].smem_for(b.rc) > (size_t)smem_optin) all[i].clear();   // staging too large
                     if (vs[i].bf16) all[i].clear();                                  // different arithmetic
+                    if (vs[i].tma && !dmaps.p) all[i].clear();                       // no tensor maps here
                 }
                 upload_tables();
                 float best = 1e30f;

@@ -24,8 +24,28 @@ struct StageArgs {
     const float* att;       // PML attenuation profiles
     int stage;              // 0..5
     int last;               // 1 at the sixth stage
-    int row_cap;            // pipelined form: floats staged per strip (>= strip length + 2, multiple of 4)
+    int row_cap;            // pipelined / staged forms: floats staged per strip (>= strip length + 2, multiple of 4)
+    // staged (TMA) form: 2-D tensor maps of every domain's fields (PSTD_TMAP_BYTES
+    // each, index (domain * 4 + field) * 4 + set, p0 as field 0 of set 3), the
+    // state-set indices of `in` and `prev`, and the word a CTA sets when a staged
+    // copy does not complete in time
+    const unsigned char* maps;
+    int set_in, set_prev;
+    int* err;
 };
+
+constexpr int PSTD_TMAP_BYTES = 128;   // sizeof(CUtensorMap)
+
+#if defined(__CUDACC__)
+#define PSTD_HD __host__ __device__
+#else
+#define PSTD_HD
+#endif
+// staged form: floats staged per strip for a bucket row cap rc (whole 16-byte
+// quads of a row job's strips, whole boxes of a column job's strips), and the
+// rows of one tensor-map box of a field with `rows` rows
+PSTD_HD constexpr int tma_cap(int rc) { return rc <= 256 ? (rc + 7) / 8 * 8 : (rc + 255) / 256 * 256; }
+PSTD_HD constexpr int tma_box_rows(int rows) { return rows < 256 ? (rows + 7) / 8 * 8 : 256; }
 
 // One compiled shape of the stage kernel for one transform length.
 struct StageVariant {
@@ -34,6 +54,8 @@ struct StageVariant {
     bool persistent;                                            // warp-specialised persistent form
     bool pipe;                                                  // pipelined persistent form (cp.async staging)
     bool bf16;                                                  // split-BF16 tensor-core DFT (precision study, opt-in)
+    int shf = 0;                                                // fused form: last radix split over a lane pair (shuffles)
+    bool tma = false;                                           // staged form: needs tensor maps and a row cap
     cudaError_t (*launch)(int n_jobs, const StageArgs& a, cudaStream_t st);
     cudaError_t (*prepare)();
     size_t (*smem_for)(int row_cap);                            // dynamic shared memory of one CTA

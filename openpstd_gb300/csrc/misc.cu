@@ -2,6 +2,8 @@
 // registry.
 #include <cuda_runtime.h>
 
+#include <vector>
+
 #include "launch.hpp"
 
 namespace pstd {
@@ -11,15 +13,56 @@ const StageVariant* stage_variants_mid(int L, int* n);
 const StageVariant* stage_variants_large(int L, int* n);
 const StageVariant* stage_variants_huge(int L, int* n);
 
+const StageVariant* stage_variants_fused_s(int L, int* n);
+const StageVariant* stage_variants_fused_m(int L, int* n);
+const StageVariant* stage_variants_fused_l(int L, int* n);
+const StageVariant* stage_variants_fused_h(int L, int* n);
+
+const StageVariant* stage_variants_tma_a(int L, int* n);
+const StageVariant* stage_variants_tma_b(int L, int* n);
+
+static const StageVariant* stage_variants_tma(int L, int* n) {
+    if (L <= 512) return stage_variants_tma_a(L, n);
+    return stage_variants_tma_b(L, n);
+}
+
+static const StageVariant* stage_variants_fused(int L, int* n) {
+    if (L <= 256) return stage_variants_fused_s(L, n);
+    if (L <= 1024) return stage_variants_fused_m(L, n);
+    if (L <= 2048) return stage_variants_fused_l(L, n);
+    return stage_variants_fused_h(L, n);
+}
+
+// Per length: the fused-form variants first (the default when nothing is
+// tuned), then the TMA-staged persistent forms, then the split gather /
+// transform / epilogue forms, then the precision-study variants.  Built once, before any launch.
 int stage_variants(int L, const StageVariant** out) {
-    int n = 0;
-    const StageVariant* v = nullptr;
-    if (L <= 256) v = stage_variants_small(L, &n);
-    else if (L <= 1024) v = stage_variants_mid(L, &n);
-    else if (L <= 2048) v = stage_variants_large(L, &n);
-    else v = stage_variants_huge(L, &n);
-    *out = v;
-    return v ? n : 0;
+    static const std::vector<std::vector<StageVariant>> lists = [] {
+        std::vector<std::vector<StageVariant>> all(14);
+        for (int lg = 0; lg < 14; lg++) {
+            const int len = 1 << lg;
+            int nf = 0, nt = 0, n = 0;
+            const StageVariant* f = stage_variants_fused(len, &nf);
+            const StageVariant* tv = stage_variants_tma(len, &nt);
+            const StageVariant* v = nullptr;
+            if (len <= 256) v = stage_variants_small(len, &n);
+            else if (len <= 1024) v = stage_variants_mid(len, &n);
+            else if (len <= 2048) v = stage_variants_large(len, &n);
+            else v = stage_variants_huge(len, &n);
+            for (int i = 0; i < nf; i++) all[lg].push_back(f[i]);
+            for (int i = 0; i < nt; i++) all[lg].push_back(tv[i]);
+            for (int i = 0; i < n; i++) all[lg].push_back(v[i]);
+        }
+        return all;
+    }();
+    *out = nullptr;
+    if (L <= 0 || (L & (L - 1)) || L >= (1 << 14)) return 0;
+    int lg = 0;
+    while ((1 << lg) < L) lg++;
+    const auto& v = lists[lg];
+    if (v.empty()) return 0;
+    *out = v.data();
+    return (int)v.size();
 }
 
 // After the sixth stage, for every PML domain (kernel/Solver.cpp:85,

@@ -115,6 +115,20 @@ static int run_frames(Kernel* k, const pstd_callbacks* cb, int save_nth = 0, int
         }
         log(PSTD_LOG_INFO, "Finished frame: " + std::to_string(p.frame));
     };
+    // frames leave the queue in frame order: saved ones after their callbacks,
+    // unsaved ones (SaveNth > 1) as soon as every earlier frame has left, so
+    // "Finished frame" is logged in frame order (kernel/Solver.cpp:86-92)
+    int inflight = 0;
+    auto pop_front = [&]() {
+        const Pending p = q.front();
+        q.pop_front();
+        if (p.slot >= 0) {
+            deliver(p);
+            inflight--;
+        } else {
+            log(PSTD_LOG_INFO, "Finished frame: " + std::to_string(p.frame));
+        }
+    };
     log(PSTD_LOG_DEBUG, "Number of render time: " + std::to_string(sc.s.calctime));
     log(PSTD_LOG_DEBUG, "Size of time step: " + std::to_string(sc.s.dt()));
     log(PSTD_LOG_INFO, "Starting simulation");
@@ -135,17 +149,23 @@ static int run_frames(Kernel* k, const pstd_callbacks* cb, int save_nth = 0, int
             if (slot_bytes) CK(cudaMemcpyAsync(base, dbase, slot_bytes, cudaMemcpyDeviceToHost, sy.copy));
             CK(cudaEventRecord(ev[s], sy.copy));
             q.push_back({f, s});
+            inflight++;
         } else {
-            log(PSTD_LOG_INFO, "Finished frame: " + std::to_string(f));
+            q.push_back({f, -1});   // logged once every earlier frame is delivered
         }
-        while ((int)q.size() >= K) { deliver(q.front()); q.pop_front(); }
+        while (!q.empty() && q.front().slot < 0 && status == PSTD_OK) pop_front();
+        while (inflight >= K && status == PSTD_OK) {
+            pop_front();
+            while (!q.empty() && q.front().slot < 0 && status == PSTD_OK) pop_front();
+        }
     }
     while (!q.empty()) {
-        if (status == PSTD_OK) deliver(q.front());
-        q.pop_front();
+        if (status == PSTD_OK) pop_front();
+        else q.pop_front();
     }
     CK(cudaStreamSynchronize(k->stream));
     CK(cudaStreamSynchronize(sy.copy));
+    k->check_stage_error();
     if (status == PSTD_OK) log(PSTD_LOG_INFO, "Succesfully finished simulation");
     else g_error = "a callback asked to stop the run";
     return status;
@@ -302,6 +322,7 @@ int pstd_synchronize(pstd_kernel* h) {
     GUARD({
         CK(cudaStreamSynchronize(h->k->stream));
         CK(cudaDeviceSynchronize());
+        h->k->check_stage_error();
         return PSTD_OK;
     })
 }
@@ -563,47 +584,18 @@ static int solve_noalloc(const pstd_config* config, int n_steps, float* frame_de
     const Scene& sc = kh.scenes[0];
     const int nd = (int)kh.gdom.size();
 
-    // field layout of pstd_create (device.cuh)
-    auto round32 = [](long long v) { return (v + 31) / 32 * 32; };
-    long long off = 0, foff = 0, poff = 0;
-    std::vector<DevDomain> hd(nd);
-    std::vector<float> att;
-    std::vector<int> pml_idx, x0, y0, frame_doms;
+    // field layout of pstd_create (device.cuh), from the same function
+    const Kernel::FieldLayout lay = kh.layout_fields();
+    const std::vector<DevDomain>& hd = lay.doms;
+    const std::vector<float>& att = lay.att;
+    const std::vector<int>& pml_idx = lay.pml_idx;
+    const long long off = (long long)lay.set_floats, foff = (long long)lay.fixed_floats, poff = (long long)lay.p0_floats;
+    std::vector<int> x0, y0, frame_doms;
     std::vector<long long> frame_off;
     long long frame_floats = 0;
     for (int k = 0; k < nd; k++) {
         const Domain& d = kh.dom(k);
-        DevDomain& h = hd[k];
-        std::memset(&h, 0, sizeof h);
-        h.nx = d.nx; h.ny = d.ny;
-        h.pitch_p = (int)round32(d.nx);
-        h.pitch_vx = (int)round32(d.nx + 1);
-        h.pitch_vy = (int)round32(d.nx);
-        h.fixed = d.rigid;
-        h.scene = 0;
-        long long& o = d.rigid ? foff : off;
-        h.o_px = o; o = round32(o + (long long)h.pitch_p * d.ny);
-        h.o_py = o; o = round32(o + (long long)h.pitch_p * d.ny);
-        h.o_vx = o; o = round32(o + (long long)h.pitch_vx * d.ny);
-        h.o_vy = o; o = round32(o + (long long)h.pitch_vy * (d.ny + 1));
-        h.o_p0 = poff; poff = round32(poff + (long long)h.pitch_p * d.ny);
-        h.rho = d.rho;
-        h.c2 = sc.s.c1 * sc.s.c1;
-        const float dt = sc.s.dt();
-        for (int i = 0; i < 6; i++) h.cdt[i] = dt * sc.s.rk[i];
-        h.pml = d.pml;
-        h.att_xp = h.att_xv = h.att_yp = h.att_yv = -1;
-        if (d.pml) {
-            pml_idx.push_back(k);
-            std::vector<double> prof;
-            auto put = [&](bool vel, bool asc, int& at) {
-                pml_profile(sc.s, vel, asc, prof);
-                at = (int)att.size();
-                for (double v : prof) att.push_back((float)v);
-            };
-            if (d.att_x) { put(false, d.asc_x, h.att_xp); put(true, d.asc_x, h.att_xv); }
-            if (d.att_y) { put(false, d.asc_y, h.att_yp); put(true, d.asc_y, h.att_yv); }
-        } else {
+        if (!d.pml) {
             frame_doms.push_back(k);
             frame_off.push_back(frame_floats);
             frame_floats += (long long)d.nx * d.ny;
@@ -611,7 +603,6 @@ static int solve_noalloc(const pstd_config* config, int n_steps, float* frame_de
         x0.push_back(d.x0);
         y0.push_back(d.y0);
     }
-    if (att.empty()) att.push_back(1.f);
 
     const int n_rec = (int)sc.receivers.size();
     if (frame_dev && frame_len < frame_floats)
@@ -637,7 +628,9 @@ static int solve_noalloc(const pstd_config* config, int n_steps, float* frame_de
         NB& b = nbs[i];
         const StageVariant* vs;
         const int nv = stage_variants(b.L, &vs);
-        for (int q = 0; q < nv && !b.var; q++) if (!vs[q].persistent) b.var = &vs[q];
+        // one CTA per job, no staging row cap, FP32 arithmetic
+        for (int q = 0; q < nv && !b.var; q++)
+            if (!vs[q].persistent && !vs[q].pipe && !vs[q].bf16 && !vs[q].tma) b.var = &vs[q];
         if (!b.var)
             return fail(PSTD_ERR_UNSUPPORTED, "strip transform length " + std::to_string(b.L) +
                                                   " is outside the compiled range 32..8192");
@@ -746,6 +739,9 @@ static int solve_noalloc(const pstd_config* config, int n_steps, float* frame_de
             a.stage = k;
             a.last = k == 5;
             a.row_cap = 0;
+            a.maps = nullptr;
+            a.set_in = a.set_prev = 0;
+            a.err = nullptr;
             for (const NB& b : nbs) {
                 a.jobs = djobs + b.off;
                 a.tw = tw + b.tw;

@@ -282,8 +282,8 @@ class PSTDKernel(KernelInterface):
         return {"ms_stage": ms.value, "ms_total": mt.value, "stage_launches": ls.value, "total_launches": lt.value}
 
     def plan_info(self) -> str:
-        buf = ctypes.create_string_buffer(8192)
-        _lib.check(_lib.lib().pstd_plan_info(self._need(), buf, 8192))
+        buf = ctypes.create_string_buffer(1 << 16)
+        _lib.check(_lib.lib().pstd_plan_info(self._need(), buf, 1 << 16))
         return buf.value.decode()
 
     def work_counts(self):

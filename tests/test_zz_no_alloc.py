@@ -74,6 +74,32 @@ def test_noalloc_matches_existing_two_calls():
 
 
 @pytest.mark.gpu
+def test_noalloc_leaves_device_memory_unchanged():
+    """After a warm-up call (which loads the kernels' modules), a further call
+    takes no device memory: the free bytes the driver reports are the same
+    before and after it, with the outputs allocated beforehand."""
+    import torch
+    from openpstd_gb300 import _lib
+    from openpstd_gb300.config import CConfig
+    a, _ = _configs()
+    steps = 12
+    want = _existing(a, steps)
+    _compare(a, steps, want)                 # warm-up: modules loaded
+    cc = CConfig(a)
+    frame = torch.empty(want[0].size, dtype=torch.float32, device="cuda")
+    rec = torch.empty(steps * want[1].shape[1], dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    rc = _lib.lib().pstd_solve_noalloc(ctypes.byref(cc.c), steps, ctypes.c_void_p(frame.data_ptr()), frame.numel(),
+                                       ctypes.c_void_p(rec.data_ptr()), rec.numel(), None)
+    _lib.check(rc)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, (free0, free1)
+    assert rel(frame.cpu().numpy(), want[0]) <= TOL
+
+
+@pytest.mark.gpu
 def test_noalloc_alternating_layouts():
     a, b = _configs()
     wa, wb = _existing(a, 10), _existing(b, 7)
