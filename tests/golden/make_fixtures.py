@@ -10,7 +10,7 @@ three large workloads, at their stated sizes:
 * ``batch``: 8 scenes of the 256-scene batched workload (seeded choice that
   always includes the largest scene), at full size, 2000 steps each;
 * ``large``: the 8192x8192 scene in 2x2 domains of 4096^2 with its 64
-  receivers placed 1-4 m from the speakers, 100 steps (the pulse moves 0.1 m
+  receivers placed 1-3 m from the speakers, 60 steps (the pulse moves 0.1 m
   per step, so every receiver records it).
 
 Each fixture ``<name>.npz`` holds, per scene ``s``:
@@ -24,9 +24,9 @@ Each fixture ``<name>.npz`` holds, per scene ``s``:
 * ``s/floor``: whole-scene relative L2 of the float oracle against FP64 per
   field (p0, px, py, vx, vy), computed here on the full fields.
 
-Run (8 host threads, about three hours on 8 cores):
+Run (8 host threads, about two and a half hours on 8 cores):
 
-    python tests/golden/make_fixtures.py [--only lshape,batch,large] [--threads 8]
+    python tests/golden/make_fixtures.py [--only batch,lshape,large] [--threads 8]
 """
 from __future__ import annotations
 
@@ -64,14 +64,21 @@ def batch_subset():
 
 def cases(only):
     out = []
-    if "lshape" in only:
+    for name in only:
+        out += _case(name)
+    return out
+
+
+def _case(name):
+    out = []
+    if name == "lshape":
         out.append(("lshape", [("lshape", scenes.l_shape(0, steps=4000), 4000, 8)]))
-    if "batch" in only:
+    if name == "batch":
         pick, confs = batch_subset()
         out.append(("batch", [(f"b{i}", confs[i], 2000, 4) for i in pick]))
-    if "large" in only:
-        conf = scenes.large_square(0, half=4096, steps=100, receivers_near=(1.0, 4.0))
-        out.append(("large", [("large", conf, 100, 0)]))
+    if name == "large":
+        conf = scenes.large_square(0, half=4096, steps=60, receivers_near=(1.0, 3.0))
+        out.append(("large", [("large", conf, 60, 0)]))
     return out
 
 
@@ -136,11 +143,11 @@ def run_scene(key, conf, steps, stride, threads, arrays, meta):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--only", default="lshape,batch,large")
+    ap.add_argument("--only", default="batch,lshape,large")
     ap.add_argument("--threads", type=int, default=os.cpu_count() or 8)
     args = ap.parse_args()
     oracle.build()
-    for name, items in cases(set(args.only.split(","))):
+    for name, items in cases(args.only.split(",")):
         arrays, meta = {}, {}
         print(f"{name}: {len(items)} scene(s)", flush=True)
         for key, conf, steps, stride in items:
