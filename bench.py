@@ -9,18 +9,30 @@ synthetic scene; the reference publishes no scenes).  A step is one full PSTD
 time step (6 RK stages) of the whole scene; the unit of work is one pressure
 cell of a non-rigid domain advanced one step.
 
-* ``value``: device-resident throughput, the K timed steps launched with
-  ``pstd_advance`` on a CUDA stream and timed with CUDA events on it.
-* ``e2e``: the same metric through the reference-facing API --
-  ``PSTDKernel.initialize_kernel`` (scene upload) + ``PSTDKernel.run`` with
-  every frame of p0 and every receiver sample delivered to host callbacks
-  (SaveNth = 1), host<->device copies included.
-* ``roofline``: the strip-pass kernel (pass_kernel<L>), 48 algorithmic bytes
-  per cell and RK stage (read px,py,vx,vy + the stage-start px,py,vx,vy, write
-  px,py,vx,vy), over its CUDA-event time measured in a second timed region
-  with events around every pass launch.
+* ``value``: device-resident throughput: K timed steps launched with
+  ``pstd_advance`` on a CUDA stream, each timed with CUDA events on it and
+  preceded by a 256 MiB write that evicts L2 (the L-shape's state is about the
+  size of L2), so every timed step reads its fields from HBM.
+* ``receiver_err``: the same scene solved for all 4000 steps on the GPU and
+  compared with the committed oracle fixture (float = the reference's CPU
+  path restated, and FP64), relative L2 of the 16 receiver series.
+* ``e2e``: the same metric through the reference-facing API: a 400-step
+  scene through ``PSTDKernel.run`` with every frame of p0 and every receiver
+  sample delivered to host callbacks (SaveNth = 1), host<->device copies in
+  the timed region; ``initialize_kernel`` (scene build, upload, plan) is timed
+  apart and reported as ``init_s``.
+* ``roofline``: the stage kernels (every strip-length bucket of an RK stage),
+  48 algorithmic bytes per cell and RK stage (read px,py,vx,vy + the
+  stage-start px,py,vx,vy, write px,py,vx,vy), over their CUDA-event time
+  measured in a second timed region with events around every stage launch.
+* ``batched``: the batched workload -- 256 scenes (total size log-uniform
+  64x64..1024x768 cells, 1-6 rectangles) advanced together -- against the
+  plain path solving the same scenes one at a time, with its receiver error on
+  the 8 fixture scenes of that workload (2000 steps).
 * ``cpu_baseline``: the CPU restatement of the reference solver (oracle/),
-  OpenMP over all host cores, on a bounded sample of the same scene.
+  OpenMP over all host cores, on a bounded sample of the same scene, with the
+  speed of its own FFT set beside scipy's pocketfft on the same strip shapes
+  (the reference links FFTW, which is absent here).
 
 ``--impl reference`` times the reference's CPU algorithm (the oracle port; the
 reference itself cannot be built: Eigen, FFTW3f, Boost and Qt5 are absent) on
@@ -43,6 +55,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 L2_BYTES = 126 * 1024 * 1024
+FLUSH_BYTES = 256 * 1024 * 1024     # written before every timed step: evicts L2
 BYTES_PER_CELL_STAGE = 48
 METRIC = "Gcell-steps/s"
 
@@ -153,12 +166,55 @@ def peaks():
 
 
 def traffic_per_cell_stage():
-    """DRAM bytes per cell and RK stage of the pass kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "pass_kernel_traffic.json")
+    """DRAM bytes per cell and RK stage of the stage kernels from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "stage_kernel_traffic.json")
     if not os.path.exists(path):
         return None, None
     d = json.load(open(path))
     return d.get("dram_bytes_per_cell_stage"), d.get("case")
+
+
+def rel(a, b):
+    import numpy as np
+    a, b = np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64)
+    n = float(np.linalg.norm(b))
+    return float(np.linalg.norm(a - b) / (n if n > 0 else 1.0))
+
+
+def fixture(name):
+    """Committed oracle fixture tests/golden/<name>.npz (float and FP64 oracle), or None."""
+    import numpy as np
+    path = os.path.join(ROOT, "tests", "golden", f"{name}.npz")
+    return np.load(path) if os.path.exists(path) else None
+
+
+def receiver_error(got, fx, key):
+    """Relative L2 of GPU receiver series against the fixture's float and FP64 oracle."""
+    r32, r64 = fx[f"{key}/rec32"], fx[f"{key}/rec64"]
+    return {"vs_f32_oracle": rel(got, r32), "vs_f64_oracle": rel(got, r64), "f32_oracle_vs_f64": rel(r32, r64)}
+
+
+def fft_speed(threads: int):
+    """The oracle's strip transform (r2c, multiply, c2r) against scipy's
+    pocketfft on the same shapes: 2048-point strips, as the L-shape's
+    1200-cell strips use."""
+    import numpy as np
+    from oracle import oracle
+    try:
+        import scipy.fft as sf
+    except ImportError:
+        return None
+    L, n = 2048, 2048
+    t_or = oracle.fft_seconds(L, n, threads, 3)
+    x = np.random.default_rng(0).random((n, L), dtype=np.float32)
+    f = np.full(L // 2 + 1, 0.5 + 0.25j, dtype=np.complex64)
+    best = 1e30
+    for _ in range(3):
+        t0 = time.perf_counter()
+        sf.irfft(sf.rfft(x, axis=1, workers=threads) * f, n=L, axis=1, workers=threads)
+        best = min(best, time.perf_counter() - t0)
+    return {"shape": f"{n} strips x {L} points, r2c + multiply + c2r", "threads": threads,
+            "oracle_ms": t_or * 1e3, "pocketfft_ms": best * 1e3, "oracle_over_pocketfft": t_or / best}
 
 
 def cpu_rate(conf, seconds: float, threads: int):
@@ -179,59 +235,92 @@ def cpu_rate(conf, seconds: float, threads: int):
     return cells * steps / el / 1e9, steps, el, cells
 
 
-def run_batch(args):
+def batch_leg(args, stream):
     """Batched workload: n independent scenes (total size log-uniform in
     64x64 .. 1024x768 cells, 1-6 rectangles, edge alpha ~ U[0,1]) advanced
-    together (value) vs the plain path solving the same scenes one at a time."""
+    together, against the plain path solving the same scenes one at a time,
+    plus the receiver error of the 8 fixture scenes of this workload advanced
+    together for 2000 steps."""
+    import numpy as np
     import torch
-    from openpstd_gb300 import build as _b, scenes
+    from openpstd_gb300 import scenes
     from openpstd_gb300.batch import BatchKernel
     from openpstd_gb300 import kernel
-    _b.build()
-    torch.cuda.set_device(0)
     confs = scenes.batch_scenes(0, n=args.batch_scenes, steps=2000)
     t0 = time.perf_counter()
     b = BatchKernel(confs)
     t_create = time.perf_counter() - t0
     cells = b.work_counts()["cells"]
-    stream = torch.cuda.Stream()
-    b.advance(args.warmup, stream.cuda_stream)
+    sh = stream.cuda_stream
+    b.advance(args.warmup, sh)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(0) as clk:
+    bsteps = max(3, min(args.steps, args.batch_steps))
+    with ClockSampler(torch.cuda.current_device()) as clk:
         e0.record(stream)
-        b.advance(args.steps, stream.cuda_stream)
+        b.advance(bsteps, sh)
         e1.record(stream)
         torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
-    batched = cells * args.steps / (ms / 1e3) / 1e9
+    batched = cells * bsteps / (ms / 1e3) / 1e9
     plan = b.plan_info().strip().splitlines()
     b.close()
-    # plain path: one scene at a time (device-resident, same steps)
-    plain_steps = max(3, min(args.steps, args.plain_steps))
+    # plain path: one scene at a time (device-resident, same step count each)
+    plain_steps = max(3, min(bsteps, args.plain_steps))
     tot_ms, tot_cells = 0.0, 0
+    t0 = time.perf_counter()
     for c in confs:
         k = kernel.PSTDKernel()
         k.initialize_kernel(c)
-        k.advance(args.warmup, stream.cuda_stream)
+        k.advance(args.warmup, sh)
         torch.cuda.synchronize()
         e0.record(stream)
-        k.advance(plain_steps, stream.cuda_stream)
+        k.advance(plain_steps, sh)
         e1.record(stream)
         torch.cuda.synchronize()
         tot_ms += e0.elapsed_time(e1)
         tot_cells += k.work_counts()["cells"] * plain_steps
         k.close()
+    t_plain = time.perf_counter() - t0
     plain = tot_cells / (tot_ms / 1e3) / 1e9
-    line = {"metric": METRIC, "value": batched, "unit": METRIC, "n_gpus": 1, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+    out = {"value": batched, "unit": METRIC, "steps": bsteps, "ms_per_step": ms / bsteps,
+           "workload": f"batch of {len(confs)} scenes, total size log-uniform 64x64..1024x768 cells, 1-6 rectangles "
+                       "each, edge alpha U[0,1], 1-4 speakers, 1-8 receivers",
+           "cells_per_step": cells, "create_s": t_create,
+           "plain_serial": {"value": plain, "unit": METRIC, "steps_per_scene": plain_steps, "wall_s": t_plain,
+                            "note": "the same scenes solved one at a time with the plain path"},
+           "batched_over_plain": batched / plain, "plan": plan, "clocks": clk.summary()}
+    fx = fixture("batch")
+    if fx is not None:
+        keys = sorted({k.split("/")[0] for k in fx.files if k.startswith("b") and k.endswith("/rec64")},
+                      key=lambda x: int(x[1:]))
+        bf = BatchKernel([confs[int(k[1:])] for k in keys])
+        bf.advance(2000, sh)
+        bf.synchronize()
+        got = np.concatenate([bf.receivers(scene=i).astype(np.float64) for i in range(len(keys))], axis=1)
+        bf.close()
+        r32 = np.concatenate([fx[f"{k}/rec32"] for k in keys], axis=1)
+        r64 = np.concatenate([fx[f"{k}/rec64"] for k in keys], axis=1)
+        out["receiver_err"] = {"scenes": [int(k[1:]) for k in keys], "steps": 2000, "vs_f32_oracle": rel(got, r32),
+                               "vs_f64_oracle": rel(got, r64), "f32_oracle_vs_f64": rel(r32, r64),
+                               "tolerance": 1e-5}
+    return out
+
+
+def run_batch(args):
+    import torch
+    from openpstd_gb300 import build as _b
+    _b.build()
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    bl = batch_leg(args, stream)
+    line = {"metric": METRIC, "value": bl["value"], "unit": METRIC, "n_gpus": 1, "steps": bl["steps"],
+            "warmup": args.warmup, "ms_per_step": bl["ms_per_step"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scenes)",
-            "config": {"workload": f"batch of {len(confs)} scenes, total size log-uniform 64x64..1024x768 cells, "
-                                   "1-6 rectangles each, edge alpha U[0,1], 1-4 speakers, 1-8 receivers",
-                       "cells_per_step": cells, "create_s": t_create},
-            "plain_serial": {"value": plain, "unit": METRIC, "steps_per_scene": plain_steps,
-                             "note": "the same scenes solved one at a time with the plain path"},
-            "batched_over_plain": batched / plain, "plan": plan, "clocks": clk.summary()}
+            "config": {"workload": bl["workload"], "cells_per_step": bl["cells_per_step"], "create_s": bl["create_s"],
+                       "l2": "no flush: 256 scenes of state (several GB) exceed L2"},
+            "plain_serial": bl["plain_serial"], "batched_over_plain": bl["batched_over_plain"],
+            "receiver_err": bl.get("receiver_err"), "plan": bl["plan"], "clocks": bl["clocks"]}
     print(json.dumps(line), flush=True)
 
 
@@ -345,7 +434,8 @@ def run_reference(args):
             "dtype": "f32", "data": "synthetic (seeded scene)", "impl": "reference",
             "config": {"workload": desc, "cells_per_step": cells, "steps_requested": args.steps},
             "cpu_baseline": {"value": v, "unit": METRIC, "cores": threads, "kind": "port",
-                             "sample": f"{done} time steps of the workload (capped at 90 s)"},
+                             "sample": f"{done} time steps of the workload (capped at 90 s)",
+                             "fft_speed": fft_speed(threads)},
             "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -372,20 +462,26 @@ def run_ours(args):
         if dist:
             dist.barrier()
 
-    # ---- device-resident timed region
+    # ---- device-resident timed region: every timed step follows a write of
+    # FLUSH_BYTES on the same stream (outside its events) that evicts L2
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     k.advance(args.warmup, sh)
     torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
-        e0.record(stream)
-        k.advance(args.steps, sh)
-        e1.record(stream)
+        with torch.cuda.stream(stream):
+            for i, (a, b) in enumerate(evs):
+                flush.fill_(float(i & 7))
+                a.record(stream)
+                k.advance(1, sh)
+                b.record(stream)
         torch.cuda.synchronize()
     barrier()
-    ms = e0.elapsed_time(e1)
+    ms = sum(a.elapsed_time(b) for a, b in evs)
     clocks = clk.summary()
+    del flush
     ms, total_cells = replica_totals(ms, cells, dist)
     value = total_cells * args.steps / (ms / 1e3) / 1e9
 
@@ -407,8 +503,20 @@ def run_ours(args):
                 "traffic_source": tcase, "stage_share_of_step": stage_ms / prof["ms_total"],
                 "plan": k.plan_info().strip().splitlines()}
 
+    # ---- receiver error: the full 4000-step solve against the committed oracle fixture
+    rec_err = None
+    fx = fixture("lshape") if args.workload == "lshape" and rank == 0 and not args.no_parity else None
+    if fx is not None:
+        kp = kernel.PSTDKernel()
+        kp.initialize_kernel(conf)
+        nsteps = int(fx["lshape/rec64"].shape[0])
+        kp.advance(nsteps, sh)
+        kp.synchronize()
+        rec_err = dict(receiver_error(kp.receivers(), fx, "lshape"), steps=nsteps, tolerance=1e-5)
+        kp.close()
+
     # ---- end-to-end through the reference-facing API (host callbacks)
-    e2e_steps = min(args.steps, 400, max(5, int(4e8 // cells)))   # every frame goes to the host
+    e2e_steps = args.e2e_steps   # every frame goes to the host
     ce = conf.copy()
     dt = ce.Settings.GetTimeStep()
     ce.Settings.SetRenderTime(float(np.float32((e2e_steps + 0.5) * float(dt))))
@@ -427,6 +535,9 @@ def run_ours(args):
     t0 = time.perf_counter()
     ke = kernel.PSTDKernel()
     ke.initialize_kernel(ce)
+    torch.cuda.synchronize()
+    init_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
     ke.run(Sink())
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
@@ -436,24 +547,30 @@ def run_ours(args):
     e2e = {"value": total_cells * e2e_steps / e2e_s / 1e9, "unit": METRIC,
            "h2d_bytes_per_step": cfg_bytes / e2e_steps,
            "d2h_bytes_per_step": (sizes["frame_bytes"] + sizes["sample_bytes"]) / e2e_steps,
-           "steps": e2e_steps, "path": "PSTDKernel.initialize_kernel + run(WriteFrame every frame, WriteSample)"}
+           "steps": e2e_steps, "init_s": init_s,
+           "with_init": total_cells * e2e_steps / (e2e_s + init_s) / 1e9,
+           "path": "PSTDKernel.run(WriteFrame every frame, WriteSample), after initialize_kernel (timed apart: init_s)"}
 
+    batched = batch_leg(args, stream) if (args.workload == "lshape" and ws == 1 and not args.no_batch) else None
     if rank != 0:
         return
-    state_bytes = 3 * 4 * cells * 5
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene, no published scene exists)",
             "config": {"workload": desc, "cells_per_step_per_gpu": cells, "air_cells": wc["air_cells"],
                        "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
-                       "l2": f"no flush: resident state {state_bytes / 2**20:.0f} MiB (3 sets x 5 fields) > L2",
+                       "l2": f"flushed: a {FLUSH_BYTES >> 20} MiB write before every timed step (outside its events)",
                        "cuda_graphs": "one graph per time step (3-phase set rotation)"},
-            "roofline": roofline, "e2e": e2e, "clocks": clocks,
+            "receiver_err": rec_err, "roofline": roofline, "e2e": e2e, "clocks": clocks,
             "gpu_launches": wc["launches_per_step"] * args.steps}
+    if batched is not None:
+        line["batched"] = batched
     if ws == 1 and not args.no_cpu_baseline:
-        v, steps, el, ccells = cpu_rate(conf, args.cpu_seconds, os.cpu_count() or 1)
-        line["cpu_baseline"] = {"value": v, "unit": METRIC, "cores": os.cpu_count() or 1, "kind": "port",
-                                "sample": f"{steps} time steps of the same scene in {el:.1f} s (oracle, OpenMP)"}
+        threads = os.cpu_count() or 1
+        v, steps, el, ccells = cpu_rate(conf, args.cpu_seconds, threads)
+        line["cpu_baseline"] = {"value": v, "unit": METRIC, "cores": threads, "kind": "port",
+                                "sample": f"{steps} time steps of the same scene in {el:.1f} s (oracle, OpenMP)",
+                                "fft_speed": fft_speed(threads)}
     print(json.dumps(line), flush=True)
 
 
@@ -467,7 +584,11 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch-scenes", type=int, default=256)
-    ap.add_argument("--plain-steps", type=int, default=50)
+    ap.add_argument("--plain-steps", type=int, default=20)
+    ap.add_argument("--batch-steps", type=int, default=200, help="timed steps of the batched leg")
+    ap.add_argument("--e2e-steps", type=int, default=400, help="steps of the end-to-end leg")
+    ap.add_argument("--no-batch", action="store_true", help="leave the batched leg out of the default line")
+    ap.add_argument("--no-parity", action="store_true", help="leave the 4000-step receiver check out")
     ap.add_argument("--rate", type=float, default=50.0, help="serve: mean request arrivals per second")
     ap.add_argument("--duration", type=float, default=60.0, help="serve: seconds of wall clock")
     ap.add_argument("--budget-gb", type=float, default=80.0, help="serve: HBM budget")

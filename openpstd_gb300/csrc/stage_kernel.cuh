@@ -189,9 +189,12 @@ struct DFT<32, INV> {
 // Plain form: L, complex strips per CTA, threads, min CTAs per SM, radices.
 // Persistent form (NTP > 0): NT FFT threads + NTP memory threads.
 // TC = 1: radix-16 passes as split-BF16 tensor-core GEMMs (precision study).
-template <int L_, int CS_, int NT_, int MINB_, int R0_, int R1_, int R2_ = 0, int R3_ = 0, int NTP_ = 0, int TC_ = 0>
+// ILP = 1: the transform passes load two butterflies before computing either
+// (shared-memory stores of one butterfly do not hold back the other's loads).
+template <int L_, int CS_, int NT_, int MINB_, int R0_, int R1_, int R2_ = 0, int R3_ = 0, int NTP_ = 0, int TC_ = 0,
+          int ILP_ = 0>
 struct Cfg {
-    static constexpr int L = L_, CS = CS_, NT = NT_, MINB = MINB_, NTP = NTP_, TC = TC_;
+    static constexpr int L = L_, CS = CS_, NT = NT_, MINB = MINB_, NTP = NTP_, TC = TC_, ILP = ILP_;
     static constexpr int R0 = R0_, R1 = R1_, R2 = R2_, R3 = R3_;
     static constexpr int NP = R3_ ? 4 : (R2_ ? 3 : 2);
     static_assert(R0 * R1 * (R2 ? R2 : 1) * (R3 ? R3 : 1) == L, "radix plan must multiply to L");
@@ -456,12 +459,144 @@ __device__ __forceinline__ void mid_pass_tc(float2* sm, const float2* filt, int 
     }
 }
 
+// Two butterflies per thread and iteration: every load of both is issued
+// before either is computed (the compiler cannot move a load above a shared
+// store of the previous butterfly, so the one-at-a-time loop leaves a
+// thread with a single butterfly's loads in flight).
+template <class C, int R, int M>
+__device__ __forceinline__ float2* pass_base(float2* sm, int it, int& n1) {
+    constexpr int Q = M / R;
+    const int cs = it % C::CS, b = it / C::CS;
+    n1 = b % Q;
+    return sm + cs * C::SP + (b / Q) * M + n1;
+}
+
+template <class C, int R, int M, int TOFF, int NTH, bool SMT, bool PRUNE>
+__device__ __forceinline__ void fwd_pass_x2(float2* sm, const float2* tw, int tid, int lim) {
+    constexpr int Q = M / R;
+    constexpr int ITEMS = C::CS * (C::L / R);
+    for (int it0 = tid; it0 < ITEMS; it0 += 2 * NTH) {
+        float2 x[2][R];
+        float2* base[2];
+        int n1[2];
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            base[u] = pass_base<C, R, M>(sm, it0 + u * NTH, n1[u]);
+#pragma unroll
+            for (int q = 0; q < R; q++)
+                x[u][q] = (!PRUNE || n1[u] + q * Q < lim) ? base[u][q * Q] : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            DFT<R, false>::run(x[u]);
+            if (Q > 1) {
+                float2 w[R];
+                load_twiddles<R, SMT>(tw + TOFF + n1[u] * R, w);
+#pragma unroll
+                for (int k = 1; k < R; k++) x[u][k] = cmul(x[u][k], w[k]);
+            }
+#pragma unroll
+            for (int k = 0; k < R; k++) base[u][k * Q] = x[u][k];
+        }
+    }
+}
+
+template <class C, int R, int M, int TOFF, int NTH, bool SMT, bool PRUNE>
+__device__ __forceinline__ void inv_pass_x2(float2* sm, const float2* tw, int tid, int lo, int hi) {
+    constexpr int Q = M / R;
+    constexpr int ITEMS = C::CS * (C::L / R);
+    for (int it0 = tid; it0 < ITEMS; it0 += 2 * NTH) {
+        float2 x[2][R];
+        float2* base[2];
+        int n1[2];
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            base[u] = pass_base<C, R, M>(sm, it0 + u * NTH, n1[u]);
+#pragma unroll
+            for (int k = 0; k < R; k++) x[u][k] = base[u][k * Q];
+        }
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            if (Q > 1) {
+                float2 w[R];
+                load_twiddles<R, SMT>(tw + TOFF + n1[u] * R, w);
+#pragma unroll
+                for (int k = 1; k < R; k++) x[u][k] = cmulc(x[u][k], w[k]);
+            }
+            DFT<R, true>::run(x[u]);
+#pragma unroll
+            for (int q = 0; q < R; q++)
+                if (!PRUNE || (n1[u] + q * Q >= lo && n1[u] + q * Q < hi)) base[u][q * Q] = x[u][q];
+        }
+    }
+}
+
+// RM: rotation mask of mid_pass (position pairs rotated by the block index)
+template <class C, int R, int NTH, bool SMT, int RM>
+__device__ __forceinline__ void mid_pass_x2(float2* sm, const float2* filt, int tid) {
+    constexpr int ITEMS = C::CS * (C::L / R);
+    for (int it0 = tid; it0 < ITEMS; it0 += 2 * NTH) {
+        float2 x[2][R];
+        float2* base[2];
+        int blk[2];
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            const int it = it0 + u * NTH;
+            const int cs = it % C::CS;
+            blk[u] = it / C::CS;
+            base[u] = sm + cs * C::SP + blk[u] * R;
+            if constexpr (RM == 0) {
+#pragma unroll
+                for (int q = 0; q < R; q++) x[u][q] = base[u][q];
+            } else {
+                const int rot = 2 * (blk[u] & RM);
+#pragma unroll
+                for (int h = 0; h < R / 2; h++) {
+                    const float4 v = *reinterpret_cast<const float4*>(base[u] + ((2 * h + rot) & (R - 1)));
+                    x[u][2 * h] = make_float2(v.x, v.y);
+                    x[u][2 * h + 1] = make_float2(v.z, v.w);
+                }
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            DFT<R, false>::run(x[u]);
+#pragma unroll
+            for (int h = 0; h < R / 2; h++) {
+                const float4 v = tload<SMT>(reinterpret_cast<const float4*>(filt + blk[u] * R) + h);
+                x[u][2 * h] = cmul(x[u][2 * h], make_float2(v.x, v.y));
+                x[u][2 * h + 1] = cmul(x[u][2 * h + 1], make_float2(v.z, v.w));
+            }
+            DFT<R, true>::run(x[u]);
+            if constexpr (RM == 0) {
+#pragma unroll
+                for (int q = 0; q < R; q++) base[u][q] = x[u][q];
+            } else {
+                const int rot = 2 * (blk[u] & RM);
+#pragma unroll
+                for (int h = 0; h < R / 2; h++)
+                    *reinterpret_cast<float4*>(base[u] + ((2 * h + rot) & (R - 1))) =
+                        make_float4(x[u][2 * h].x, x[u][2 * h].y, x[u][2 * h + 1].x, x[u][2 * h + 1].y);
+            }
+        }
+    }
+}
+
+template <class C, int R, int NTH>
+__host__ __device__ constexpr bool use_x2() {
+    return C::ILP && !C::TC && R <= 16 && (C::CS * (C::L / R)) % (2 * NTH) == 0;
+}
+
 // PRUNE (first pass, M = L): positions at or past `lim` hold the zero padding
 // and are not loaded (nor stored by the gather)
 template <class C, int R, int M, int TOFF, int NTH, bool SMT, bool PRUNE = false>
 __device__ __forceinline__ void fwd_pass(float2* sm, const float2* tw, int tid, int lim = 0) {
     if constexpr (C::TC && R == 16) {
         fwd_pass_tc<C, M, TOFF, NTH, SMT>(sm, tw, tid);
+        return;
+    }
+    if constexpr (use_x2<C, R, NTH>()) {
+        fwd_pass_x2<C, R, M, TOFF, NTH, SMT, PRUNE>(sm, tw, tid, lim);
         return;
     }
     constexpr int Q = M / R;
@@ -511,6 +646,10 @@ __device__ __forceinline__ void inv_pass(float2* sm, const float2* tw, int tid, 
         inv_pass_tc<C, M, TOFF, NTH, SMT>(sm, tw, tid);
         return;
     }
+    if constexpr (use_x2<C, R, NTH>()) {
+        inv_pass_x2<C, R, M, TOFF, NTH, SMT, PRUNE>(sm, tw, tid, lo, hi);
+        return;
+    }
     constexpr int Q = M / R;
     constexpr int ITEMS = C::CS * (C::L / R);
     for (int it = tid; it < ITEMS; it += NTH) {
@@ -557,6 +696,10 @@ template <class C, int R, int NTH, bool SMT>
 __device__ __forceinline__ void mid_pass(float2* sm, const float2* filt, int tid) {
     if constexpr (C::TC && R == 16) {
         mid_pass_tc<C, NTH, SMT>(sm, filt, tid);
+        return;
+    }
+    if constexpr (use_x2<C, R, NTH>()) {
+        mid_pass_x2<C, R, NTH, SMT, mid_rot_mask<C, R>()>(sm, filt, tid);
         return;
     }
     constexpr int ITEMS = C::CS * (C::L / R);

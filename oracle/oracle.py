@@ -65,6 +65,7 @@ def lib():
         L.orc_spatderp3.argtypes = [P(f64), i32, P(f64), i32, P(f64), i32, P(f64), i32, P(f64), i32,
                                     f64, f64, f64, i32, i32, P(f64)]
         L.orc_max_threads.restype = i32
+        L.orc_fft_seconds.argtypes = [i32, i32, i32, i32, P(f64)]
         _lib = L
     return _lib
 
@@ -201,3 +202,11 @@ def spatderp3(p1, p2, p3, derfact, window_coeffs, wlen, rho1, rho_self, rho2, ve
 
 def max_threads() -> int:
     return lib().orc_max_threads()
+
+
+def fft_seconds(L: int, n_strips: int, threads: int, reps: int = 3) -> float:
+    """Seconds for n_strips real strips of length L through the oracle's own
+    r2c -> multiply -> c2r (the transform core of its strip derivative)."""
+    out = ctypes.c_double()
+    _check(lib().orc_fft_seconds(L, n_strips, threads, reps, ctypes.byref(out)))
+    return out.value

@@ -1152,6 +1152,40 @@ int orc_spatderp3(const double* p1, int32_t n1, const double* p2, int32_t n2, co
     catch (OracleError& e) { g_err = e.what(); return e.code; }
 }
 
+// Speed of the oracle's own strip transform (float): n_strips strips of
+// length L through r2c, a complex multiply per bin and c2r -- the transform
+// core of spatderp3 -- on `threads` OpenMP threads, best of `reps` runs.  Lets
+// a caller set the oracle's FFT beside another FFT library on the same shapes,
+// so the oracle's speed is not read as FFTW's.
+int32_t orc_fft_seconds(int32_t L, int32_t n_strips, int32_t threads, int32_t reps, double* seconds) {
+    if (L < 4 || (L & (L - 1)) || n_strips < 1 || threads < 1 || reps < 1 || !seconds) {
+        g_err = "orc_fft_seconds: bad arguments";
+        return PSTD_ERR_INVALID;
+    }
+    std::vector<float> data((size_t)n_strips * L);
+    for (size_t i = 0; i < data.size(); i++) data[i] = (float)((i * 2654435761u) % 1000) * 1e-3f;
+    std::vector<std::complex<float>> filt(L / 2 + 1, std::complex<float>(0.5f, 0.25f));
+    double best = 1e30;
+    for (int r = 0; r < reps; r++) {
+        const double t0 = omp_get_wtime();
+#pragma omp parallel num_threads(threads)
+        {
+            const RealFFT<float>& plan = fft_plan<float>(L);
+            std::vector<std::complex<float>> spec(L / 2 + 1), work(L / 2 + 1);
+#pragma omp for schedule(static)
+            for (int s = 0; s < n_strips; s++) {
+                float* x = data.data() + (size_t)s * L;
+                plan.r2c(x, spec.data(), work.data());
+                for (int k = 0; k <= L / 2; k++) spec[k] *= filt[k];
+                plan.c2r(spec.data(), x, work.data());
+            }
+        }
+        best = std::min(best, omp_get_wtime() - t0);
+    }
+    *seconds = best;
+    return 0;
+}
+
 int32_t orc_max_threads(void) {
 #ifdef _OPENMP
     return omp_get_max_threads();

@@ -1,0 +1,140 @@
+"""GPU solves at the workloads' stated sizes against committed oracle fixtures.
+
+The fixtures (``tests/golden/{lshape,batch,large}.npz``, written by
+``tests/golden/make_fixtures.py``) hold the float oracle (the reference's CPU
+PSTDKernel restated in its own precision) and the FP64 oracle run on:
+
+* the L-shaped 3-domain scene, all 4000 steps, 16 receivers;
+* 8 scenes of the 256-scene batched workload at full size, 2000 steps each
+  (solved alone and together in one batch);
+* the 8192x8192 scene in 2x2 domains, 60 steps, 64 receivers 1-3 m from the
+  speakers.
+
+Tolerances (relative L2):
+* receiver series: <= 1e-5 against the FP64 oracle, or <= 3x the float
+  oracle's own distance to FP64 (+1e-6) where that distance is above 1e-5/3;
+  and <= 1e-5 against the float oracle wherever the float oracle is within
+  1e-5/3 of FP64;
+* final p0, px, py, vx, vy on the stored windows: within 3x the float
+  oracle's distance to FP64 on the same windows (+1e-6).
+
+With PSTD_PARITY_REPORT=<path> every test appends its measured errors to that
+file as JSON lines.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from parity import FIELDS, rel
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+REC_TOL = 1e-5
+
+
+def _fixture(name):
+    path = os.path.join(GOLDEN, f"{name}.npz")
+    if not os.path.exists(path):
+        pytest.skip(f"fixture {name}.npz not generated (tests/golden/make_fixtures.py)")
+    return np.load(path)
+
+
+def _report(entry):
+    path = os.environ.get("PSTD_PARITY_REPORT")
+    print(json.dumps(entry))
+    if path:
+        with open(path, "a") as f:
+            f.write(json.dumps(entry) + "\n")
+
+
+def _check(fx, key, receivers, snapshot, label):
+    """Compare one scene's GPU receivers and final fields with fixture `key`."""
+    r32, r64 = fx[f"{key}/rec32"].astype(np.float64), fx[f"{key}/rec64"]
+    rg = np.asarray(receivers, dtype=np.float64)
+    assert rg.shape == r64.shape, (rg.shape, r64.shape)
+    out = {"case": label, "steps": int(r64.shape[0]), "receivers": int(r64.shape[1]),
+           "rec_vs_f32": rel(rg, r32), "rec_vs_f64": rel(rg, r64), "rec_f32_vs_f64": rel(r32, r64)}
+    fields = {}
+    for f in FIELDS:
+        got, want64, want32 = [], [], []
+        for row in fx[f"{key}/win"]:
+            i, r0, r1, rs, c0, c1, cs = (int(v) for v in row)
+            a = np.asarray(snapshot(i, f))
+            got.append(a[r0:r1:rs, c0:c1:cs].astype(np.float64).ravel())
+            want64.append(fx[f"{key}/{i}/{f}/64"].astype(np.float64).ravel())
+            want32.append(fx[f"{key}/{i}/{f}/32"].astype(np.float64).ravel())
+        g, w64, w32 = np.concatenate(got), np.concatenate(want64), np.concatenate(want32)
+        fields[f] = {"vs_f64": rel(g, w64), "vs_f32": rel(g, w32), "f32_vs_f64": rel(w32, w64)}
+    out["fields"] = fields
+    out["fields_whole_scene_f32_vs_f64"] = dict(zip(FIELDS, (float(x) for x in fx[f"{key}/floor"])))
+    _report(out)
+    floor = out["rec_f32_vs_f64"]
+    assert out["rec_vs_f64"] <= max(REC_TOL, 3 * floor + 1e-6), out
+    if floor <= REC_TOL / 3:
+        assert out["rec_vs_f32"] <= REC_TOL, out
+    for f, e in fields.items():
+        assert e["vs_f64"] <= 3 * e["f32_vs_f64"] + 1e-6, (f, e)
+    return out
+
+
+def _solve(conf, steps):
+    from openpstd_gb300 import kernel
+    k = kernel.PSTDKernel()
+    k.initialize_kernel(conf)
+    k.advance(steps)
+    k.synchronize()
+    return k
+
+
+def test_lshape_4000_steps():
+    """The L-shaped scene at full size for all 4000 steps."""
+    from openpstd_gb300 import scenes
+    fx = _fixture("lshape")
+    k = _solve(scenes.l_shape(0, steps=4000), 4000)
+    _check(fx, "lshape", k.receivers(), k.snapshot, "lshape 1200x600+600x600+600x1200, 4000 steps")
+    k.close()
+
+
+def _batch_keys(fx):
+    return sorted({k.split("/")[0] for k in fx.files if k.startswith("b") and k.endswith("/rec64")},
+                  key=lambda s: int(s[1:]))
+
+
+def test_batch_scenes_full_size_solo():
+    """Eight scenes of the batched workload at full size, 2000 steps, each solved alone."""
+    from openpstd_gb300 import scenes
+    fx = _fixture("batch")
+    confs = scenes.batch_scenes(0, n=256, steps=2000)
+    for key in _batch_keys(fx):
+        k = _solve(confs[int(key[1:])], 2000)
+        _check(fx, key, k.receivers(), k.snapshot, f"batch scene {key[1:]} alone, 2000 steps")
+        k.close()
+
+
+def test_batch_scenes_full_size_together():
+    """The same eight scenes advanced together in one batch (strip-length buckets
+    shared across scenes) match the oracle as well."""
+    from openpstd_gb300 import scenes
+    from openpstd_gb300.batch import BatchKernel
+    fx = _fixture("batch")
+    confs = scenes.batch_scenes(0, n=256, steps=2000)
+    keys = _batch_keys(fx)
+    b = BatchKernel([confs[int(k[1:])] for k in keys])
+    b.advance(2000)
+    b.synchronize()
+    for si, key in enumerate(keys):
+        _check(fx, key, b.receivers(scene=si), lambda i, f, si=si: b.scene_snapshot(si, i, f),
+               f"batch scene {key[1:]} in a batch of {len(keys)}, 2000 steps")
+    b.close()
+
+
+def test_large_8192():
+    """The 8192x8192 scene (2x2 domains of 4096^2, L = 8192 strips), 60 steps."""
+    from openpstd_gb300 import scenes
+    fx = _fixture("large")
+    k = _solve(scenes.large_square(0, half=4096, steps=60, receivers_near=(1.0, 3.0)), 60)
+    _check(fx, "large", k.receivers(), k.snapshot, "8192x8192 in 2x2 domains, 60 steps")
+    k.close()
