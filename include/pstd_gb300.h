@@ -44,6 +44,7 @@ extern "C" {
 #define PSTD_ERR_NO_MEMORY      6  /* device or pinned host allocation failed / over budget */
 #define PSTD_ERR_CANCELLED      7  /* request cancelled */
 #define PSTD_ERR_TIMEOUT        8  /* a bounded device wait gave up */
+#define PSTD_ERR_IO             9  /* the scene file's key/value store failed (see pstd_file_last_error) */
 
 /* ---- log levels (KernelCallbackLog, kernel/KernelInterface.h:243-271) --- */
 #define PSTD_LOG_FATAL   0
@@ -304,6 +305,45 @@ int pstd_server_stats(pstd_server* s, int64_t* stats);
 #define PSTD_NOALLOC_SCRATCH_BYTES (16u << 20)
 int pstd_solve_noalloc(const pstd_config* config, int32_t n_steps, float* frame_dev, int64_t frame_len,
                        float* receivers_dev, int64_t receivers_len, void* stream);
+
+/* ---- scene files (.pstd) -------------------------------------------------
+ * The reference's PSTDFile (shared/PSTDFile.h:161-415, shared/PSTDFile.cpp):
+ * an unqlite key/value file holding the scene configuration (a Boost text
+ * archive of PSTDConfiguration), per-domain result frames and per-receiver
+ * samples under int32 keys {prefix, indices...}.  unqlite is loaded at run
+ * time from `unqlite_lib` (NULL: $PSTD_UNQLITE_LIB, else "libunqlite.so"),
+ * the shared library the reference builds from its unqlite/unqlite.c.
+ * Errors: PSTD_ERR_INVALID (bad argument, missing record, malformed archive),
+ * PSTD_ERR_UNSUPPORTED (library missing, wrong file version -- the
+ * reference's PSTDFileVersionException), PSTD_ERR_IO (store failure --
+ * PSTDFileIOException); pstd_file_last_error() has the message. */
+typedef struct pstd_file pstd_file;
+/* PSTDFile::Open (create_new = 0; the file must hold version 4) or
+ * PSTDFile::New (create_new = 1: version, CreateDefaultConf scene, empty
+ * results scene, committed) -- shared/PSTDFile.cpp:168-205 */
+int pstd_file_open(const char* path, const char* unqlite_lib, int32_t create_new, pstd_file** out);
+void pstd_file_close(pstd_file* f);   /* unqlite_close commits pending changes */
+/* GetSceneConf / GetResultsSceneConf (results = 1); the arrays `out` points
+ * into stay valid until the next call of this function or pstd_file_close */
+int pstd_file_get_scene(pstd_file* f, int32_t results, pstd_config* out);
+/* SetSceneConf (results = 0) or the results-scene record (results = 1) */
+int pstd_file_set_scene(pstd_file* f, int32_t results, const pstd_config* config);
+int pstd_file_initialize_results(pstd_file* f);   /* InitializeResults (:234-249) */
+int pstd_file_delete_results(pstd_file* f);       /* DeleteResults (:251-266) */
+/* SaveNextResultsFrame: appends frame (count)++ of `domain` (:227-232) */
+int pstd_file_save_frame(pstd_file* f, int32_t domain, const float* data, int64_t n);
+int pstd_file_frame_count(pstd_file* f, int32_t domain, int32_t* count);   /* GetResultsFrameCount */
+/* GetResultsFrame: *n = floats in the record; at most cap copied to dst (dst may be NULL) */
+int pstd_file_get_frame(pstd_file* f, int32_t domain, int32_t frame, float* dst, int64_t cap, int64_t* n);
+int pstd_file_append_samples(pstd_file* f, int32_t receiver, const float* data, int64_t n);   /* SaveReceiverData */
+int pstd_file_get_samples(pstd_file* f, int32_t receiver, float* dst, int64_t cap, int64_t* n);   /* GetReceiverData */
+int pstd_file_commit(pstd_file* f);     /* Commit */
+int pstd_file_rollback(pstd_file* f);   /* Rollback */
+const char* pstd_file_last_error(void);
+/* The Boost text archive of `config` alone (no reference counterpart: the
+ * reference writes it inside SetSceneConf); *len = its length, at most
+ * cap - 1 bytes and a terminating 0 written to buf (buf may be NULL). */
+int pstd_archive_encode(const pstd_config* config, char* buf, int64_t cap, int64_t* len);
 
 /* ---- library ------------------------------------------------------------ */
 const char* pstd_last_error(void);

@@ -211,5 +211,48 @@ struct ConfigStorage {
     pstd_config c{};
 };
 void to_c_config(const PSTDConfiguration& conf, ConfigStorage& storage);
+std::shared_ptr<PSTDConfiguration> from_c_config(const pstd_config& c);
+
+// shared/PSTDFile.h:134-159
+class PSTDFileVersionException : public std::runtime_error {
+public:
+    explicit PSTDFileVersionException(const std::string& m) : std::runtime_error(m) {}
+};
+class PSTDFileIOException : public std::runtime_error {
+public:
+    int code;
+    PSTDFileIOException(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+// Scene file (.pstd) with the results of runs: shared/PSTDFile.h:161-415 on
+// the pstd_file_* C ABI.  unqlite_lib: the unqlite shared library ("" =
+// $PSTD_UNQLITE_LIB, else libunqlite.so).
+class PSTDFile {
+public:
+    static std::unique_ptr<PSTDFile> Open(const std::string& path, const std::string& unqlite_lib = "");
+    static std::unique_ptr<PSTDFile> New(const std::string& path, const std::string& unqlite_lib = "");
+    ~PSTDFile();
+    PSTDFile(const PSTDFile&) = delete;
+    PSTDFile& operator=(const PSTDFile&) = delete;
+
+    void Commit();
+    void Rollback();
+    std::shared_ptr<PSTDConfiguration> GetSceneConf();
+    void SetSceneConf(std::shared_ptr<PSTDConfiguration> scene);
+    void InitializeResults();
+    std::shared_ptr<PSTDConfiguration> GetResultsSceneConf();
+    int GetResultsDomainCount();
+    int GetResultsFrameCount(unsigned int domain);
+    PSTD_FRAME_PTR GetResultsFrame(unsigned int frame, unsigned int domain);
+    void SaveNextResultsFrame(unsigned int domain, PSTD_FRAME_PTR frame);
+    void DeleteResults();
+    void SaveReceiverData(unsigned int receiver, std::shared_ptr<std::vector<float>> data);
+    std::shared_ptr<std::vector<float>> GetReceiverData(unsigned int receiver);
+    int GetResultsReceiverCount();
+
+private:
+    explicit PSTDFile(pstd_file* h) : h_(h) {}
+    pstd_file* h_ = nullptr;
+};
 
 }  // namespace pstd_gb300

@@ -23,6 +23,7 @@ PSTD_ERR_CALLBACK = 5
 PSTD_ERR_NO_MEMORY = 6
 PSTD_ERR_CANCELLED = 7
 PSTD_ERR_TIMEOUT = 8
+PSTD_ERR_IO = 9
 
 FIELD = {"p0": 0, "px": 1, "py": 2, "vx": 3, "vy": 4}
 
@@ -74,6 +75,21 @@ SIGNATURES = {
     "pstd_server_cancel": (ctypes.c_int, [_vp, _i64]),
     "pstd_server_stats": (ctypes.c_int, [_vp, _P(_i64)]),
     "pstd_solve_noalloc": (ctypes.c_int, [_P(c_config), _i32, _vp, _i64, _vp, _i64, _vp]),
+    "pstd_file_open": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, _i32, _P(_vp)]),
+    "pstd_file_close": (None, [_vp]),
+    "pstd_file_get_scene": (ctypes.c_int, [_vp, _i32, _P(c_config)]),
+    "pstd_file_set_scene": (ctypes.c_int, [_vp, _i32, _P(c_config)]),
+    "pstd_file_initialize_results": (ctypes.c_int, [_vp]),
+    "pstd_file_delete_results": (ctypes.c_int, [_vp]),
+    "pstd_file_save_frame": (ctypes.c_int, [_vp, _i32, _P(_f32), _i64]),
+    "pstd_file_frame_count": (ctypes.c_int, [_vp, _i32, _P(_i32)]),
+    "pstd_file_get_frame": (ctypes.c_int, [_vp, _i32, _i32, _P(_f32), _i64, _P(_i64)]),
+    "pstd_file_append_samples": (ctypes.c_int, [_vp, _i32, _P(_f32), _i64]),
+    "pstd_file_get_samples": (ctypes.c_int, [_vp, _i32, _P(_f32), _i64, _P(_i64)]),
+    "pstd_file_commit": (ctypes.c_int, [_vp]),
+    "pstd_file_rollback": (ctypes.c_int, [_vp]),
+    "pstd_file_last_error": (ctypes.c_char_p, []),
+    "pstd_archive_encode": (ctypes.c_int, [_P(c_config), ctypes.c_char_p, _i64, _P(_i64)]),
     "pstd_last_error": (ctypes.c_char_p, []),
     "pstd_version": (ctypes.c_char_p, []),
 }

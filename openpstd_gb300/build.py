@@ -18,7 +18,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpstd_gb300.so")
 
 SOURCES = ["scene.cpp", "stage_fused_s.cu", "stage_fused_m.cu", "stage_fused_l.cu", "stage_fused_h.cu", "stage_tma_a.cu", "stage_tma_b.cu", "stage_small.cu", "stage_mid.cu", "stage_large.cu", "stage_huge.cu", "stage_all.cu", "misc.cu", "solver.cu", "server.cu",
-           "gpu_pstd_kernel.cpp"]
+           "gpu_pstd_kernel.cpp", "pstdfile.cpp"]
 HEADERS = ["scene.hpp", "device.cuh", "launch.hpp", "stage_kernel.cuh", "stage_fused.cuh", "stage_tma.cuh", "kernel_state.hpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
@@ -57,7 +57,7 @@ def build(verbose: bool = False) -> str:
     with cf.ThreadPoolExecutor(max_workers=len(srcs)) as ex:
         objs = list(ex.map(_compile, srcs))
     if not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs):
-        cmd = [NVCC, "-shared", "-o", LIB + ".tmp"] + objs + ARCH + ["-lcudart"]
+        cmd = [NVCC, "-shared", "-o", LIB + ".tmp"] + objs + ARCH + ["-lcudart", "-ldl"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -233,3 +233,113 @@ std::vector<float> GpuPSTDKernel::receivers(int first_step, int n_steps) {
 }
 
 }  // namespace pstd_gb300
+
+namespace pstd_gb300 {
+
+std::shared_ptr<PSTDConfiguration> from_c_config(const pstd_config& c) {
+    auto conf = std::make_shared<PSTDConfiguration>();
+    PSTDSettings& s = conf->Settings;
+    const pstd_settings& x = c.settings;
+    s.calctime = x.calctime; s.c1 = x.c1; s.ampMax = x.ampMax; s.freqMax = x.freqMax; s.rho = x.rho;
+    s.patcherror = x.patcherror; s.tfactRK = x.tfactRK; s.gridSpacing = x.gridSpacing;
+    s.band_width = x.band_width; s.wave_length = x.wave_length;
+    s.rk_coefficients.assign(x.rk_coefficients, x.rk_coefficients + (x.n_rk_coefficients > 6 ? 6 : x.n_rk_coefficients));
+    s.spectral_interpolation = x.spectral_interpolation != 0;
+    s.PMLCells = x.PMLCells;
+    s.SaveNth = x.SaveNth;
+    for (int i = 0; i < c.n_speakers; i++)
+        conf->Speakers.push_back(Vec3(c.speakers[3 * i], c.speakers[3 * i + 1], c.speakers[3 * i + 2]));
+    for (int i = 0; i < c.n_receivers; i++)
+        conf->Receivers.push_back(Vec3(c.receivers[3 * i], c.receivers[3 * i + 1], c.receivers[3 * i + 2]));
+    for (int i = 0; i < c.n_domains; i++) {
+        const pstd_domain_conf& d = c.domains[i];
+        DomainConf o;
+        o.TopLeft = Vec2(d.top_left[0], d.top_left[1]);
+        o.Size = Vec2(d.size[0], d.size[1]);
+        o.T = {d.T.absorption, d.T.lr != 0};
+        o.L = {d.L.absorption, d.L.lr != 0};
+        o.B = {d.B.absorption, d.B.lr != 0};
+        o.R = {d.R.absorption, d.R.lr != 0};
+        conf->Domains.push_back(o);
+    }
+    return conf;
+}
+
+// status -> the reference's PSTDFile exceptions
+static void file_check(int rc) {
+    if (rc == PSTD_OK) return;
+    const std::string m = pstd_file_last_error();
+    if (rc == PSTD_ERR_UNSUPPORTED && m.rfind("Wrong version", 0) == 0) throw PSTDFileVersionException(m);
+    throw PSTDFileIOException(rc, m);
+}
+
+std::unique_ptr<PSTDFile> PSTDFile::Open(const std::string& path, const std::string& lib) {
+    pstd_file* h = nullptr;
+    file_check(pstd_file_open(path.c_str(), lib.empty() ? nullptr : lib.c_str(), 0, &h));
+    return std::unique_ptr<PSTDFile>(new PSTDFile(h));
+}
+
+std::unique_ptr<PSTDFile> PSTDFile::New(const std::string& path, const std::string& lib) {
+    pstd_file* h = nullptr;
+    file_check(pstd_file_open(path.c_str(), lib.empty() ? nullptr : lib.c_str(), 1, &h));
+    return std::unique_ptr<PSTDFile>(new PSTDFile(h));
+}
+
+PSTDFile::~PSTDFile() { pstd_file_close(h_); }
+void PSTDFile::Commit() { file_check(pstd_file_commit(h_)); }
+void PSTDFile::Rollback() { file_check(pstd_file_rollback(h_)); }
+
+std::shared_ptr<PSTDConfiguration> PSTDFile::GetSceneConf() {
+    pstd_config c{};
+    file_check(pstd_file_get_scene(h_, 0, &c));
+    return from_c_config(c);
+}
+
+std::shared_ptr<PSTDConfiguration> PSTDFile::GetResultsSceneConf() {
+    pstd_config c{};
+    file_check(pstd_file_get_scene(h_, 1, &c));
+    return from_c_config(c);
+}
+
+void PSTDFile::SetSceneConf(std::shared_ptr<PSTDConfiguration> scene) {
+    ConfigStorage st;
+    to_c_config(*scene, st);
+    file_check(pstd_file_set_scene(h_, 0, &st.c));
+}
+
+void PSTDFile::InitializeResults() { file_check(pstd_file_initialize_results(h_)); }
+void PSTDFile::DeleteResults() { file_check(pstd_file_delete_results(h_)); }
+int PSTDFile::GetResultsDomainCount() { return (int)GetResultsSceneConf()->Domains.size(); }
+int PSTDFile::GetResultsReceiverCount() { return (int)GetResultsSceneConf()->Receivers.size(); }
+
+int PSTDFile::GetResultsFrameCount(unsigned int domain) {
+    int32_t n = 0;
+    file_check(pstd_file_frame_count(h_, (int32_t)domain, &n));
+    return n;
+}
+
+PSTD_FRAME_PTR PSTDFile::GetResultsFrame(unsigned int frame, unsigned int domain) {
+    int64_t n = 0;
+    file_check(pstd_file_get_frame(h_, (int32_t)domain, (int32_t)frame, nullptr, 0, &n));
+    auto out = std::make_shared<std::vector<float>>((size_t)n);
+    file_check(pstd_file_get_frame(h_, (int32_t)domain, (int32_t)frame, out->data(), n, &n));
+    return out;
+}
+
+void PSTDFile::SaveNextResultsFrame(unsigned int domain, PSTD_FRAME_PTR frame) {
+    file_check(pstd_file_save_frame(h_, (int32_t)domain, frame->data(), (int64_t)frame->size()));
+}
+
+void PSTDFile::SaveReceiverData(unsigned int receiver, std::shared_ptr<std::vector<float>> data) {
+    file_check(pstd_file_append_samples(h_, (int32_t)receiver, data->data(), (int64_t)data->size()));
+}
+
+std::shared_ptr<std::vector<float>> PSTDFile::GetReceiverData(unsigned int receiver) {
+    int64_t n = 0;
+    file_check(pstd_file_get_samples(h_, (int32_t)receiver, nullptr, 0, &n));
+    auto out = std::make_shared<std::vector<float>>((size_t)n);
+    file_check(pstd_file_get_samples(h_, (int32_t)receiver, out->data(), n, &n));
+    return out;
+}
+
+}  // namespace pstd_gb300

@@ -25,6 +25,18 @@ sys.path.insert(0, os.path.dirname(_HERE))
 from openpstd_gb300.config import CConfig, PSTDConfiguration, c_domain_info  # noqa: E402
 
 
+REFERENCE = "/root/reference"
+
+
+def unqlite_lib():
+    """Path of the reference's unqlite store built into oracle/_ref (make), or
+    None where the reference tree is absent."""
+    out = os.path.join(_HERE, "_ref", "libunqlite.so")
+    if os.path.exists(os.path.join(REFERENCE, "unqlite", "unqlite.c")):
+        subprocess.check_call(["make", "-s", "-C", _HERE, "_ref/libunqlite.so", f"REF={REFERENCE}"])
+    return out if os.path.exists(out) else None
+
+
 def build(force: bool = False) -> str:
     """Compile the oracle with g++ (OpenMP on)."""
     if force or not os.path.exists(_LIB) or os.path.getmtime(_LIB) < os.path.getmtime(_SRC):

@@ -46,3 +46,19 @@ def test_cxx_api_run_matches_oracle(driver, oracle_mod):
     want = s.receivers()
     assert got.shape == want.shape
     assert np.linalg.norm(got - want) / np.linalg.norm(want) < 1e-5
+
+
+def test_cxx_pstdfile(pstd_lib, tmp_path):
+    """pstd_gb300::PSTDFile (the reference's PSTDFile class on the C ABI),
+    used from C++ over the reference's unqlite store."""
+    from oracle import oracle
+    unq = oracle.unqlite_lib()
+    if unq is None:
+        pytest.skip("the reference's unqlite source is not available")
+    exe = str(tmp_path / "pstdfile_driver")
+    libdir = os.path.join(ROOT, "openpstd_gb300")
+    subprocess.check_call(["g++", "-std=c++17", "-O1", "-o", exe, os.path.join(ROOT, "tests", "cxx", "pstdfile_driver.cpp"),
+                           "-I" + os.path.join(ROOT, "include"), "-L" + libdir, "-lpstd_gb300", "-Wl,-rpath," + libdir])
+    out = json.loads(subprocess.check_output([exe, str(tmp_path / "scene.pstd"), unq]))
+    assert out == {"domains": 2, "receivers": 2, "results_domains": 2, "frames": 3, "frame2": 1.0, "samples": 2,
+                   "sample0": 1.25, "open_missing_throws": True, "pml": 50, "window": 32}
