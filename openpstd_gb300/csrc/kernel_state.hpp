@@ -208,7 +208,7 @@ struct Kernel {
     std::vector<float2> filt;
     std::map<std::tuple<int, int, int, int, int, int, float>, int> filt_off;   // (L, vel, radices, dx)
     std::vector<float2> tw;
-    std::map<std::tuple<int, int, int, int, int, int>, int> tw_off;   // (L, radices, lane-pair split)
+    std::map<std::tuple<int, int, int, int, int, int>, int> tw_off;   // (L, radices, lane-pair split / computed twiddles)
 
     // frames
     std::vector<int> frame_doms;
@@ -299,19 +299,31 @@ struct Kernel {
     // holds [n1][k] = exp(-2 pi i n1 k / M) for n1 < M/R, k < R; the offset
     // of every pass is a multiple of 2 float2 (16-byte loads)
     int twiddles_of(const StageVariant* v) {
-        auto key = std::make_tuple(v->L, v->r[0], v->r[1], v->r[2], v->r[3], v->shf);
+        auto key = std::make_tuple(v->L, v->r[0], v->r[1], v->r[2], v->r[3], v->shf * 2 + v->ctw);
         auto it = tw_off.find(key);
         if (it != tw_off.end()) return it->second;
         if (tw.size() & 1) tw.push_back(make_float2(0, 0));
         int o = (int)tw.size();
         int M = v->L;
+        auto put = [&](double n, int M_) {
+            double a = -2.0 * M_PI * n / M_;
+            tw.push_back(make_float2((float)std::cos(a), (float)std::sin(a)));
+        };
         for (int p = 0; p + 1 < v->np; p++) {
             const int R = v->r[p], Q = M / R;
-            for (int n1 = 0; n1 < Q; n1++)
-                for (int k = 0; k < R; k++) {
-                    double a = -2.0 * M_PI * (double)n1 * k / M;
-                    tw.push_back(make_float2((float)std::cos(a), (float)std::sin(a)));
+            for (int n1 = 0; n1 < Q; n1++) {
+                if (!v->ctw) {
+                    for (int k = 0; k < R; k++) put((double)n1 * k, M);
+                } else if (R >= 16) {   // the powers make_twiddles multiplies out (stage_kernel.cuh)
+                    put(n1, M); put(2.0 * n1, M); put(4.0 * n1, M); put(8.0 * n1, M);
+                } else if (R == 8) {
+                    put(n1, M); put(4.0 * n1, M);
+                } else if (R == 4) {
+                    put(n1, M); put(2.0 * n1, M);
+                } else {
+                    put(n1, M); put(n1, M);
                 }
+            }
             M = Q;
         }
         if (v->shf) {

@@ -56,6 +56,7 @@ struct StageVariant {
     bool bf16;                                                  // split-BF16 tensor-core DFT (precision study, opt-in)
     int shf = 0;                                                // fused form: last radix split over a lane pair (shuffles)
     bool tma = false;                                           // staged form: needs tensor maps and a row cap
+    int ctw = 0;                                                // twiddle tables hold powers (Cfg::CTW)
     cudaError_t (*launch)(int n_jobs, const StageArgs& a, cudaStream_t st);
     cudaError_t (*prepare)();
     size_t (*smem_for)(int row_cap);                            // dynamic shared memory of one CTA

@@ -402,7 +402,7 @@ __device__ __forceinline__ void fused_mid_radix(float2* sm, const float2* tw, co
 template <class C, int NTH>
 __device__ __forceinline__ void fused_middle(float2* sm, const float2* tw, const float2* filt, int tid) {
     constexpr int M1 = C::M1, M2 = C::M2;
-    constexpr int T1 = C::L, T2 = C::L + C::M1;
+    constexpr int T1 = C::T1, T2 = C::T2;
     if constexpr (C::NP == 2) {
         fused_mid_radix<C, C::R1, NTH>(sm, tw, filt, tid);
     } else if constexpr (C::NP == 3) {

@@ -185,16 +185,25 @@ struct DFT<32, INV> {
     }
 };
 
+// Computed twiddles: float2 read per butterfly for radix R -- (w, w^2, w^4,
+// w^8) for R = 16, (w, w^4) for R = 8, (w, w^2) for R = 4, (w, w) for R = 2;
+// the rest are products of at most three of them (make_twiddles).
+__host__ __device__ constexpr int tw_entry(int R) { return R >= 16 ? 4 : 2; }
+
 // ---------------------------------------------------------------- variants
 // Plain form: L, complex strips per CTA, threads, min CTAs per SM, radices.
 // Persistent form (NTP > 0): NT FFT threads + NTP memory threads.
 // TC = 1: radix-16 passes as split-BF16 tensor-core GEMMs (precision study).
 // ILP = 1: the transform passes load two butterflies before computing either
 // (shared-memory stores of one butterfly do not hold back the other's loads).
+// CTW = 1: the twiddles of a pass are formed in registers from a few powers
+// read from the table (tw_entry below) instead of read one by one: the
+// table loads through L1 were the largest share of the transform passes' L1
+// traffic.
 template <int L_, int CS_, int NT_, int MINB_, int R0_, int R1_, int R2_ = 0, int R3_ = 0, int NTP_ = 0, int TC_ = 0,
-          int ILP_ = 0>
+          int ILP_ = 0, int CTW_ = 0>
 struct Cfg {
-    static constexpr int L = L_, CS = CS_, NT = NT_, MINB = MINB_, NTP = NTP_, TC = TC_, ILP = ILP_;
+    static constexpr int L = L_, CS = CS_, NT = NT_, MINB = MINB_, NTP = NTP_, TC = TC_, ILP = ILP_, CTW = CTW_;
     static constexpr int R0 = R0_, R1 = R1_, R2 = R2_, R3 = R3_;
     static constexpr int NP = R3_ ? 4 : (R2_ ? 3 : 2);
     static_assert(R0 * R1 * (R2 ? R2 : 1) * (R3 ? R3 : 1) == L, "radix plan must multiply to L");
@@ -205,7 +214,12 @@ struct Cfg {
     static constexpr int BUF = CS * SP;            // float2 per job buffer
     // twiddle table: one [n1][k] block of M entries per pass but the last
     static constexpr int M1 = L / R0, M2 = M1 / R1;
-    static constexpr int TWN = NP == 2 ? L : (NP == 3 ? L + M1 : L + M1 + M2);
+    // float2 per butterfly row of a pass's table: R (one per twiddle) or, with
+    // CTW, the powers tw_entry<R>() lists
+    static constexpr int TE0 = CTW ? tw_entry(R0) : R0, TE1 = CTW ? tw_entry(R1) : R1, TE2 = CTW ? tw_entry(R2 ? R2 : 1) : R2;
+    static constexpr int T1 = (L / R0) * TE0;                   // offset of pass 1's table
+    static constexpr int T2 = T1 + (M1 / R1) * TE1;             // offset of pass 2's table
+    static constexpr int TWN = NP == 2 ? T1 : (NP == 3 ? T2 : T2 + (R2 ? (M2 / R2) * TE2 : 0));
     static constexpr int SMEM = NTP ? (2 * BUF + TWN + 2 * L) * 8 : BUF * 8;
 };
 
@@ -236,6 +250,42 @@ __device__ __forceinline__ void load_twiddles(const float2* row, float2 (&w)[R])
         w[2 * h] = make_float2(v.x, v.y);
         w[2 * h + 1] = make_float2(v.z, v.w);
     }
+}
+
+// w[k] = w^k, k < R, from the row of powers tw_entry<R> lists (FP64-built);
+// no product chains more than three roundings
+template <int R, bool SMT>
+__device__ __forceinline__ void make_twiddles(const float2* row, float2 (&w)[R]) {
+    const float4* t4 = reinterpret_cast<const float4*>(row);
+    const float4 a = tload<SMT>(t4);
+    const float2 w1 = make_float2(a.x, a.y), wb = make_float2(a.z, a.w);
+    w[0] = make_float2(1.f, 0.f);
+    if constexpr (R == 2) {
+        w[1] = w1;
+    } else if constexpr (R == 4) {
+        w[1] = w1;
+        w[2] = wb;
+        w[3] = cmul(wb, w1);
+    } else if constexpr (R == 8) {
+        const float2 w2 = cmul(w1, w1), w3 = cmul(w2, w1);
+        w[1] = w1; w[2] = w2; w[3] = w3; w[4] = wb;
+        w[5] = cmul(wb, w1); w[6] = cmul(wb, w2); w[7] = cmul(wb, w3);
+    } else {
+        static_assert(R == 16, "computed twiddles for radix 2..16");
+        const float4 b = tload<SMT>(t4 + 1);
+        const float2 w2 = wb, w4 = make_float2(b.x, b.y), w8 = make_float2(b.z, b.w);
+        const float2 w3 = cmul(w2, w1), w12 = cmul(w8, w4);
+        w[1] = w1; w[2] = w2; w[3] = w3; w[4] = w4;
+        w[5] = cmul(w4, w1); w[6] = cmul(w4, w2); w[7] = cmul(w4, w3); w[8] = w8;
+        w[9] = cmul(w8, w1); w[10] = cmul(w8, w2); w[11] = cmul(w8, w3); w[12] = w12;
+        w[13] = cmul(w12, w1); w[14] = cmul(w12, w2); w[15] = cmul(w12, w3);
+    }
+}
+
+template <class C, int R, bool SMT>
+__device__ __forceinline__ void pass_twiddles(const float2* tab, int n1, float2 (&w)[R]) {
+    if constexpr (C::CTW) make_twiddles<R, SMT>(tab + n1 * tw_entry(R), w);
+    else load_twiddles<R, SMT>(tab + n1 * R, w);
 }
 
 // ---------------------------------------------------------------- split-BF16 DFT-16 on tensor cores
@@ -491,7 +541,7 @@ __device__ __forceinline__ void fwd_pass_x2(float2* sm, const float2* tw, int ti
             DFT<R, false>::run(x[u]);
             if (Q > 1) {
                 float2 w[R];
-                load_twiddles<R, SMT>(tw + TOFF + n1[u] * R, w);
+                pass_twiddles<C, R, SMT>(tw + TOFF, n1[u], w);
 #pragma unroll
                 for (int k = 1; k < R; k++) x[u][k] = cmul(x[u][k], w[k]);
             }
@@ -519,7 +569,7 @@ __device__ __forceinline__ void inv_pass_x2(float2* sm, const float2* tw, int ti
         for (int u = 0; u < 2; u++) {
             if (Q > 1) {
                 float2 w[R];
-                load_twiddles<R, SMT>(tw + TOFF + n1[u] * R, w);
+                pass_twiddles<C, R, SMT>(tw + TOFF, n1[u], w);
 #pragma unroll
                 for (int k = 1; k < R; k++) x[u][k] = cmulc(x[u][k], w[k]);
             }
@@ -607,6 +657,7 @@ __device__ __forceinline__ void fwd_pass(float2* sm, const float2* tw, int tid, 
         float2* base = sm + cs * C::SP + blk * M + n1;
         float2 x[R];
         if constexpr (R == 32) {
+            static_assert(!C::CTW, "computed twiddles cover radix 2..16");
             // 32 values per thread: twiddles loaded pairwise after the butterfly
 #pragma unroll
             for (int q = 0; q < R; q++)
@@ -623,7 +674,7 @@ __device__ __forceinline__ void fwd_pass(float2* sm, const float2* tw, int tid, 
             }
         } else {
             float2 w[R];
-            if (Q > 1) load_twiddles<R, SMT>(tw + TOFF + n1 * R, w);
+            if (Q > 1) pass_twiddles<C, R, SMT>(tw + TOFF, n1, w);
 #pragma unroll
             for (int q = 0; q < R; q++)
                 x[q] = (!PRUNE || n1 + q * Q < lim) ? base[q * Q] : make_float2(0.f, 0.f);
@@ -661,6 +712,7 @@ __device__ __forceinline__ void inv_pass(float2* sm, const float2* tw, int tid, 
         for (int k = 0; k < R; k++) x[k] = base[k * Q];
         if (Q > 1) {
             if constexpr (R == 32) {
+                static_assert(!C::CTW, "computed twiddles cover radix 2..16");
                 const float4* t4 = reinterpret_cast<const float4*>(tw + TOFF + n1 * R);
 #pragma unroll
                 for (int h = 0; h < R / 2; h++) {
@@ -670,7 +722,7 @@ __device__ __forceinline__ void inv_pass(float2* sm, const float2* tw, int tid, 
                 }
             } else {
                 float2 w[R];
-                load_twiddles<R, SMT>(tw + TOFF + n1 * R, w);
+                pass_twiddles<C, R, SMT>(tw + TOFF, n1, w);
 #pragma unroll
                 for (int k = 1; k < R; k++) x[k] = cmulc(x[k], w[k]);
             }
@@ -753,7 +805,7 @@ template <class C, int NTH, int BAR, bool SMT, bool PRUNE = false>
 __device__ __forceinline__ void convolve(float2* sm, const float2* tw, const float2* filt, int tid, int z0 = 0,
                                          int lo = 0, int hi = 0) {
     constexpr int M0 = C::L, M1 = C::M1, M2 = C::M2;
-    constexpr int T0 = 0, T1 = M0, T2 = M0 + M1;
+    constexpr int T0 = 0, T1 = C::T1, T2 = C::T2;
     if constexpr (C::NP == 2) {
         fwd_pass<C, C::R0, M0, T0, NTH, SMT, PRUNE>(sm, tw, tid, z0);
         group_sync<BAR, NTH>();
@@ -1771,6 +1823,7 @@ StageVariant make_sprev_variant(const char* name) {
     v.persistent = false;
     v.pipe = true;   // needs the bucket's row cap
     v.bf16 = false;
+    v.ctw = C::CTW;
     v.launch = &launch_sprev_t<C>;
     v.prepare = &prepare_sprev_t<C>;
     v.smem_for = &sprev_smem<C>;
@@ -1823,6 +1876,7 @@ StageVariant make_pipe_variant(const char* name) {
     v.persistent = false;
     v.pipe = true;
     v.bf16 = false;
+    v.ctw = C::CTW;
     v.launch = &launch_pipe_t<C>;
     v.prepare = &prepare_pipe_t<C>;
     v.smem_for = &pipe_smem<C>;
@@ -1865,6 +1919,7 @@ StageVariant make_variant(const char* name) {
     v.persistent = C::NTP > 0;
     v.pipe = false;
     v.bf16 = C::TC != 0;
+    v.ctw = C::CTW;
     v.launch = &launch_stage_t<C>;
     v.prepare = &prepare_stage_t<C>;
     v.smem_for = &plain_smem<C>;

@@ -16,9 +16,14 @@ const StageVariant* stage_variants_large(int L, int* n) {
         make_variant<Cfg<2048, 2, 256, 4, 16, 16, 8>>("L2048 cs2 nt256 mb4 r16.16.8"),
         make_sprev_variant<Cfg<2048, 4, 256, 2, 16, 16, 8>>("L2048 cs4 nt256 sprev r16.16.8"),
         make_sprev_variant<Cfg<2048, 2, 256, 4, 16, 16, 8>>("L2048 cs2 nt256 mb4 sprev r16.16.8"),
+        make_variant<Cfg<2048, 4, 256, 3, 16, 16, 8, 0, 0, 0, 0, 1>>("L2048 cs4 nt256 r16.16.8 ctw"),
+        make_variant<Cfg<2048, 4, 256, 2, 16, 16, 8, 0, 0, 0, 1, 1>>("L2048 cs4 nt256 mb2 r16.16.8 ilp ctw"),
+        make_variant<Cfg<2048, 4, 256, 3, 8, 8, 8, 4, 0, 0, 0, 1>>("L2048 cs4 nt256 r8.8.8.4 ctw"),
+        make_variant<Cfg<2048, 2, 256, 4, 16, 16, 8, 0, 0, 0, 0, 1>>("L2048 cs2 nt256 mb4 r16.16.8 ctw"),
+        make_sprev_variant<Cfg<2048, 4, 256, 2, 16, 16, 8, 0, 0, 0, 0, 1>>("L2048 cs4 nt256 sprev r16.16.8 ctw"),
     };
     switch (L) {
-        case 2048: *n = 11; return v2048;
+        case 2048: *n = 16; return v2048;
         default: *n = 0; return nullptr;
     }
 }

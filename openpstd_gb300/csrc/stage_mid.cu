@@ -12,6 +12,9 @@ const StageVariant* stage_variants_mid(int L, int* n) {
         make_variant<Cfg<512, 8, 256, 4, 8, 8, 8>>("L512 cs8 nt256 mb4 r8.8.8"),
         make_variant<Cfg<512, 8, 128, 4, 32, 16>>("L512 cs8 nt128 mb4 r32.16"),
         make_sprev_variant<Cfg<512, 8, 256, 3, 8, 8, 8>>("L512 cs8 nt256 sprev r8.8.8"),
+        make_variant<Cfg<512, 8, 256, 4, 8, 8, 8, 0, 0, 0, 0, 1>>("L512 cs8 nt256 mb4 r8.8.8 ctw"),
+        make_variant<Cfg<512, 8, 256, 3, 16, 8, 4, 0, 0, 0, 0, 1>>("L512 cs8 nt256 r16.8.4 ctw"),
+        make_sprev_variant<Cfg<512, 8, 256, 3, 8, 8, 8, 0, 0, 0, 0, 1>>("L512 cs8 nt256 sprev r8.8.8 ctw"),
     };
     static const StageVariant v1024[] = {
         make_variant<Cfg<1024, 8, 256, 3, 16, 8, 8>>("L1024 cs8 nt256 r16.8.8"),
@@ -28,10 +31,15 @@ const StageVariant* stage_variants_mid(int L, int* n) {
         make_sprev_variant<Cfg<1024, 4, 256, 3, 16, 8, 8>>("L1024 cs4 nt256 sprev r16.8.8"),
         make_sprev_variant<Cfg<1024, 4, 256, 4, 16, 8, 8>>("L1024 cs4 nt256 mb4 sprev r16.8.8"),
         make_sprev_variant<Cfg<1024, 8, 256, 2, 32, 32>>("L1024 cs8 nt256 mb2 sprev r32.32"),
+        make_variant<Cfg<1024, 4, 256, 3, 16, 8, 8, 0, 0, 0, 0, 1>>("L1024 cs4 nt256 r16.8.8 ctw"),
+        make_variant<Cfg<1024, 8, 256, 3, 16, 8, 8, 0, 0, 0, 0, 1>>("L1024 cs8 nt256 r16.8.8 ctw"),
+        make_variant<Cfg<1024, 8, 256, 2, 16, 8, 8, 0, 0, 0, 1, 1>>("L1024 cs8 nt256 mb2 r16.8.8 ilp ctw"),
+        make_variant<Cfg<1024, 4, 256, 4, 16, 8, 8, 0, 0, 0, 0, 1>>("L1024 cs4 nt256 mb4 r16.8.8 ctw"),
+        make_sprev_variant<Cfg<1024, 4, 256, 3, 16, 8, 8, 0, 0, 0, 0, 1>>("L1024 cs4 nt256 sprev r16.8.8 ctw"),
     };
     switch (L) {
-        case 512: *n = 7; return v512;
-        case 1024: *n = 14; return v1024;
+        case 512: *n = 10; return v512;
+        case 1024: *n = 19; return v1024;
         default: *n = 0; return nullptr;
     }
 }

@@ -18,6 +18,10 @@ const StageVariant* stage_variants_small(int L, int* n) {
         make_pipe_variant<Cfg<128, 8, 64, 4, 16, 8>>("L128 cs8 pipe64 r16.8"),
         make_variant<Cfg<128, 16, 128, 8, 16, 8>>("L128 cs16 nt128 mb8 r16.8"),
         make_sprev_variant<Cfg<128, 16, 128, 6, 16, 8>>("L128 cs16 nt128 sprev r16.8"),
+        make_variant<Cfg<128, 16, 128, 6, 16, 8, 0, 0, 0, 0, 0, 1>>("L128 cs16 nt128 r16.8 ctw"),
+        make_variant<Cfg<128, 16, 128, 8, 16, 8, 0, 0, 0, 0, 0, 1>>("L128 cs16 nt128 mb8 r16.8 ctw"),
+        make_sprev_variant<Cfg<128, 16, 128, 6, 16, 8, 0, 0, 0, 0, 0, 1>>("L128 cs16 nt128 sprev r16.8 ctw"),
+        make_pipe_variant<Cfg<128, 8, 64, 4, 16, 8, 0, 0, 0, 0, 0, 1>>("L128 cs8 pipe64 r16.8 ctw"),
     };
     static const StageVariant v256[] = {
         make_variant<Cfg<256, 16, 256, 3, 16, 16>>("L256 cs16 nt256 r16.16"),
@@ -26,12 +30,15 @@ const StageVariant* stage_variants_small(int L, int* n) {
         make_pipe_variant<Cfg<256, 8, 128, 2, 16, 16>>("L256 cs8 pipe128 r16.16"),
         make_variant<Cfg<256, 16, 256, 4, 16, 16>>("L256 cs16 nt256 mb4 r16.16"),
         make_sprev_variant<Cfg<256, 16, 256, 3, 16, 16>>("L256 cs16 nt256 sprev r16.16"),
+        make_variant<Cfg<256, 16, 256, 4, 16, 16, 0, 0, 0, 0, 0, 1>>("L256 cs16 nt256 mb4 r16.16 ctw"),
+        make_variant<Cfg<256, 8, 128, 5, 16, 16, 0, 0, 0, 0, 0, 1>>("L256 cs8 nt128 r16.16 ctw"),
+        make_sprev_variant<Cfg<256, 16, 256, 3, 16, 16, 0, 0, 0, 0, 0, 1>>("L256 cs16 nt256 sprev r16.16 ctw"),
     };
     switch (L) {
         case 32: *n = 1; return v32;
         case 64: *n = 1; return v64;
-        case 128: *n = 7; return v128;
-        case 256: *n = 6; return v256;
+        case 128: *n = 11; return v128;
+        case 256: *n = 9; return v256;
         default: *n = 0; return nullptr;
     }
 }

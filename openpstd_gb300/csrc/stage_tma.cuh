@@ -525,6 +525,7 @@ StageVariant make_tma_variant(const char* name) {
     v.pipe = false;
     v.bf16 = false;
     v.tma = true;
+    v.ctw = C::CTW;
     v.launch = &launch_tma_t<C>;
     v.prepare = &prepare_tma_t<C>;
     v.smem_for = &tma_smem<C>;
