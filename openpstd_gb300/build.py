@@ -16,6 +16,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpstd_gb300.so")
+CLI = os.path.join(HERE, "pstd-cli")
 
 SOURCES = ["scene.cpp", "stage_fused_s.cu", "stage_fused_m.cu", "stage_fused_l.cu", "stage_fused_h.cu", "stage_tma_a.cu", "stage_tma_b.cu", "stage_small.cu", "stage_mid.cu", "stage_large.cu", "stage_huge.cu", "stage_all.cu", "misc.cu", "solver.cu", "server.cu",
            "gpu_pstd_kernel.cpp", "pstdfile.cpp"]
@@ -62,6 +63,17 @@ def build(verbose: bool = False) -> str:
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
         os.replace(LIB + ".tmp", LIB)
+    # the command line (CLI/main.cpp's create / run), linked against the library
+    cli_src = os.path.join(CSRC, "pstd_cli.cpp")
+    hdr = os.path.join(ROOT, "include", "pstd_kernel.hpp")
+    if not os.path.exists(CLI) or os.path.getmtime(CLI) < max(os.path.getmtime(LIB), os.path.getmtime(cli_src),
+                                                              os.path.getmtime(hdr)):
+        cmd = [os.environ.get("CXX", "g++"), "-std=c++17", "-O2", "-o", CLI + ".tmp", cli_src,
+               "-I" + os.path.join(ROOT, "include"), "-L" + HERE, "-lpstd_gb300", "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"pstd-cli build failed:\n{r.stdout}\n{r.stderr}")
+        os.replace(CLI + ".tmp", CLI)
     if verbose:
         print("built", LIB)
     return LIB

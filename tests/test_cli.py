@@ -90,3 +90,42 @@ def test_cli_run_gpu_and_device_subsampling(tmp_path):
         nx, ny = md.DomainMetadata[d][:2]
         full = got_f[(d, f)].reshape(ny, nx)        # row-major, x fastest
         assert np.array_equal(data, full[::2, ::2].ravel())
+
+
+def _cxx_cli(*args, unq=None):
+    exe = os.path.join(ROOT, "openpstd_gb300", "pstd-cli")
+    env = dict(os.environ)
+    if unq:
+        env["PSTD_UNQLITE_LIB"] = unq
+    return subprocess.run([exe, *args], capture_output=True, text=True, env=env)
+
+
+def test_cxx_cli_create_and_run_stand_in(pstd_lib, tmp_path):
+    """The C++ command line (pstd-cli, CLI/main.cpp's create and RunCommand)
+    on a .pstd scene file: `create` writes the default scene; `run -M` runs
+    RunCommand's sequence with the stand-in kernel and the frames and samples
+    land in the file; `run` without -g is refused (no CPU solver)."""
+    from oracle import oracle
+    from openpstd_gb300.config import PSTDConfiguration
+    from openpstd_gb300.pstdfile import PSTDFile
+    unq = oracle.unqlite_lib()
+    if unq is None:
+        pytest.skip("the reference's unqlite source is not available")
+    p = str(tmp_path / "scene.pstd")
+    r = _cxx_cli("create", p, unq=unq)
+    assert r.returncode == 0, r.stderr
+    conf = PSTDConfiguration.CreateDefaultConf()
+    conf.Settings.SetRenderTime(float(np.float32(3.5 * conf.Settings.GetTimeStep())))   # 3 frames
+    with PSTDFile.Open(p, unq) as f:
+        f.SetSceneConf(conf)
+        f.Commit()
+    r = _cxx_cli("run", p, unq=unq)
+    assert r.returncode == 1 and "-g" in r.stderr
+    r = _cxx_cli("run", "-f", p, "-M", unq=unq)
+    assert r.returncode == 0, r.stderr
+    assert "Delete old results" in r.stdout and "Finished the stand-in kernel" in r.stdout
+    with PSTDFile.Open(p, unq) as f:
+        assert f.GetResultsDomainCount() == 2
+        assert f.GetResultsFrameCount(0) == 3 and f.GetResultsFrameCount(1) == 3
+        assert np.array_equal(f.GetResultsFrame(2, 1), np.full(100 * 75, 2.0, np.float32))   # 20 m x 15 m at 0.2 m
+        assert np.array_equal(f.GetReceiverData(0), [0.0, 1.0, 2.0])
