@@ -93,11 +93,20 @@ static std::vector<int> bin_positions(int L, const int* r, int np) {
     return pos;
 }
 
-// PSTD_DFT=bf16x3 selects the split-BF16 tensor-core DFT variants for the
-// strip lengths that have one (precision study); the default is FP32
-inline bool want_bf16_dft() {
+// PSTD_DFT selects a tensor-core DFT precision study for the strip lengths
+// that have one: "bf16x3" (split BF16 on mma.sync) or "tf32x3" (split TF32 on
+// tcgen05 with TMEM accumulators); the default is the FP32 FFT
+inline std::string study_dft() {
     const char* e = std::getenv("PSTD_DFT");
-    return e && std::string(e) == "bf16x3";
+    return e ? std::string(e) : std::string();
+}
+inline bool want_bf16_dft() {
+    const std::string s = study_dft();
+    return s == "bf16x3" || s == "tf32x3";
+}
+inline bool study_variant_matches(const StageVariant& v) {
+    const std::string s = study_dft();
+    return v.bf16 && ((s == "tf32x3") == v.tc5);
 }
 
 // the FP32 variants come first in every list; the study variants follow
@@ -548,7 +557,12 @@ struct Kernel {
             if (b.var->smem_for(b.rc) > (size_t)smem_optin) b.var = &vs[0];   // pinned form does not fit
             if (want_bf16_dft())
                 for (int i = 0; i < nv; i++)
-                    if (vs[i].bf16) { b.var = &vs[i]; b.choice = " split-BF16 DFT (precision study)"; b.pinned = true; }
+                    if (study_variant_matches(vs[i])) {
+                        b.var = &vs[i];
+                        b.choice = vs[i].tc5 ? " split-TF32 tcgen05 DFT (precision study)"
+                                             : " split-BF16 DFT (precision study)";
+                        b.pinned = true;
+                    }
             if (int i = planned_variant(L); i >= 0 && i < nv_fp32) {
                 b.var = &vs[i];
                 b.choice = " pinned by PSTD_PLAN";

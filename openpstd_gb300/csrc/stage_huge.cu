@@ -1,5 +1,5 @@
 // stage kernel variants for transform lengths 4096 and 8192
-#include "stage_kernel.cuh"
+#include "stage_tc5.cuh"
 
 namespace pstd {
 
@@ -23,10 +23,11 @@ const StageVariant* stage_variants_huge(int L, int* n) {
         make_variant<Cfg<8192, 2, 512, 1, 16, 16, 8, 4, 0, 0, 0, 1>>("L8192 cs2 nt512 r16.16.8.4 ctw"),
         make_variant<Cfg<8192, 1, 256, 2, 16, 16, 8, 4, 0, 0, 1, 1>>("L8192 cs1 nt256 mb2 r16.16.8.4 ilp ctw"),
         make_variant<Cfg<8192, 1, 256, 2, 16, 16, 16, 2, 0, 1>>("L8192 cs1 nt256 r16.16.16.2 bf16x3"),
+        make_tc5_variant<Cfg<8192, 1, 256, 1, 16, 16, 16, 2>>("L8192 cs1 nt256 r16.16.16.2 tcgen05 tf32x3"),
     };
     switch (L) {
         case 4096: *n = 8; return v4096;
-        case 8192: *n = 8; return v8192;
+        case 8192: *n = 9; return v8192;
         default: *n = 0; return nullptr;
     }
 }
