@@ -1,6 +1,7 @@
 """Throughput of the GB300 PSTD solve (Gcell-steps/s).
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload lshape|square|batch|serve]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                   [--workload lshape|square|square1200|rect8192|large|batch|serve]
 
 Workload (default ``lshape``): the multi-domain L-shaped scene -- 1200x600,
 600x600 and 600x1200 air cells (dx = 0.2 m) with a seeded mix of rigid and
@@ -75,6 +76,9 @@ def workload(name: str, seed: int):
         conf.Speakers = [(120.05, 130.05, 0.0)]
         conf.Receivers = [(200.05, 150.05, 0.0)]
         return conf, "square 1200x1200 cells, rigid edges (transform length 2048 only), 1 speaker, 1 receiver"
+    if name == "rect8192":
+        return scenes.rect(6 + seed, nx=4100, ny=1200, steps=1000), (
+            "rectangle 4100x1200 cells + 50-cell PML (transform length 8192 along x), 1 speaker, 2 receivers")
     if name == "large":
         return scenes.large_square(seed, half=4096, steps=1000), (
             "8192x8192 cells as 2x2 domains of 4096x4096 with windowed interfaces, 50-cell PML (alpha 1) on the "
@@ -186,6 +190,24 @@ def fixture(name):
     import numpy as np
     path = os.path.join(ROOT, "tests", "golden", f"{name}.npz")
     return np.load(path) if os.path.exists(path) else None
+
+
+def parity_case(workload: str):
+    """(fixture key, scene factory, description) of the full-size oracle
+    fixture that belongs to a workload, or None."""
+    from openpstd_gb300 import scenes
+    if workload == "lshape":
+        return "lshape", lambda: scenes.l_shape(0, steps=4000), "the benchmarked scene, all 4000 steps"
+    if workload == "large":
+        return ("large", lambda: scenes.large_square(0, half=4096, steps=60, receivers_near=(1.0, 3.0)),
+                "the 8192^2 scene with its 64 receivers 1-3 m from the speakers, 60 steps")
+    return None
+
+
+def dft_form():
+    return {"tf32x3": "split-TF32 tcgen05 DFT (precision study, L=8192 strips)",
+            "bf16x3": "split-BF16 mma.sync DFT (precision study, L=4096/8192 strips)"}.get(
+        os.environ.get("PSTD_DFT", ""), "FP32 FFT")
 
 
 def receiver_error(got, fx, key):
@@ -503,20 +525,22 @@ def run_ours(args):
                 "traffic_source": tcase, "stage_share_of_step": stage_ms / prof["ms_total"],
                 "plan": k.plan_info().strip().splitlines()}
 
-    # ---- receiver error: the full 4000-step solve against the committed oracle fixture
+    # ---- receiver error: the workload's full-size solve against its committed oracle fixture
     rec_err = None
-    fx = fixture("lshape") if args.workload == "lshape" and rank == 0 and not args.no_parity else None
+    parity = parity_case(args.workload)
+    fx = fixture(parity[0]) if parity and rank == 0 and not args.no_parity else None
     if fx is not None:
         kp = kernel.PSTDKernel()
-        kp.initialize_kernel(conf)
-        nsteps = int(fx["lshape/rec64"].shape[0])
+        kp.initialize_kernel(parity[1]())
+        nsteps = int(fx[f"{parity[0]}/rec64"].shape[0])
         kp.advance(nsteps, sh)
         kp.synchronize()
-        rec_err = dict(receiver_error(kp.receivers(), fx, "lshape"), steps=nsteps, tolerance=1e-5)
+        rec_err = dict(receiver_error(kp.receivers(), fx, parity[0]), steps=nsteps, tolerance=1e-5,
+                       scene=parity[2])
         kp.close()
 
     # ---- end-to-end through the reference-facing API (host callbacks)
-    e2e_steps = args.e2e_steps   # every frame goes to the host
+    e2e_steps = max(5, min(args.e2e_steps, int(2e9 // cells)))   # every frame goes to the host
     ce = conf.copy()
     dt = ce.Settings.GetTimeStep()
     ce.Settings.SetRenderTime(float(np.float32((e2e_steps + 0.5) * float(dt))))
@@ -560,7 +584,7 @@ def run_ours(args):
             "config": {"workload": desc, "cells_per_step_per_gpu": cells, "air_cells": wc["air_cells"],
                        "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
                        "l2": f"flushed: a {FLUSH_BYTES >> 20} MiB write before every timed step (outside its events)",
-                       "cuda_graphs": "one graph per time step (3-phase set rotation)"},
+                       "cuda_graphs": "one graph per time step (3-phase set rotation)", "dft": dft_form()},
             "receiver_err": rec_err, "roofline": roofline, "e2e": e2e, "clocks": clocks,
             "gpu_launches": wc["launches_per_step"] * args.steps}
     if batched is not None:
