@@ -75,7 +75,7 @@ def _case(name):
         out.append(("lshape", [("lshape", scenes.l_shape(0, steps=4000), 4000, 8)]))
     if name == "batch":
         pick, confs = batch_subset()
-        out.append(("batch", [(f"b{i}", confs[i], 2000, 4) for i in pick]))
+        out.append(("batch", [(f"b{i}", confs[i], 2000, 8) for i in pick]))
     if name == "large":
         conf = scenes.large_square(0, half=4096, steps=60, receivers_near=(1.0, 3.0))
         out.append(("large", [("large", conf, 60, 0)]))
