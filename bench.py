@@ -346,48 +346,112 @@ def run_batch(args):
     print(json.dumps(line), flush=True)
 
 
+def request_cells(conf) -> int:
+    """Non-rigid cells of a scene, PML domains included: the work of one of
+    its steps in the unit the server counts (scene built on the host)."""
+    import ctypes
+    from openpstd_gb300 import _lib
+    from openpstd_gb300.config import CConfig, c_domain_info
+    cc, h = CConfig(conf), ctypes.c_void_p()
+    _lib.check(_lib.lib().pstd_scene_build(ctypes.byref(cc.c), ctypes.byref(h)))
+    try:
+        n, total = ctypes.c_int32(), 0
+        _lib.check(_lib.lib().pstd_scene_domain_count(h, ctypes.byref(n)))
+        for i in range(n.value):
+            d = c_domain_info()
+            _lib.check(_lib.lib().pstd_scene_domain_info(h, i, ctypes.byref(d)))
+            if not d.is_rigid:
+                total += d.size[0] * d.size[1]
+        return total
+    finally:
+        _lib.lib().pstd_destroy(h)
+
+
+TICK_SECONDS = 0.25
+
+
+def serve_leg(reqs, duration, budget, tick_steps):
+    """Feed a request stream (arrival time, scene) to a fresh server for
+    `duration` seconds of wall clock; latency = completion - arrival.  Ticks
+    are sized to about TICK_SECONDS of wall clock (at most tick_steps steps),
+    so that arrivals are admitted within that time however large the batch."""
+    from openpstd_gb300.serving import Server
+    work = [request_cells(c) * c.Settings.framecount() for _, c in reqs]   # built before the clock starts
+    srv = Server(budget, max_scenes=4096)
+    pending, live, offered, steps = 0, {}, 0, tick_steps
+    lat, occ = [], []
+    t0 = time.perf_counter()
+    while True:
+        now = time.perf_counter() - t0
+        if now >= duration:
+            break
+        while pending < len(reqs) and reqs[pending][0] <= now:
+            at, conf = reqs[pending]
+            rid = srv.submit(conf, conf.Settings.framecount())
+            offered += work[pending]
+            live[rid] = at
+            pending += 1
+        t_tick = time.perf_counter()
+        info = srv.tick(steps)
+        if info["steps"]:
+            # next tick: about TICK_SECONDS of wall clock, at most tick_steps steps
+            per_step = (time.perf_counter() - t_tick) / info["steps"]
+            steps = max(1, min(tick_steps, int(TICK_SECONDS / max(per_step, 1e-6))))
+        occ.append(srv.stats()["bytes_in_use"])
+        if info["finished"]:
+            t_done = time.perf_counter() - t0
+            for rid in list(live):
+                if srv.poll(rid)["state"] == 2:
+                    lat.append(t_done - live.pop(rid))
+                    srv.result(rid)
+        if info["active"] == 0 and info["queued"] == 0 and pending < len(reqs):
+            time.sleep(max(0.0, min(reqs[pending][0] - (time.perf_counter() - t0), 0.01)))
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    lat_s = sorted(lat)
+    pct = (lambda q: lat_s[min(len(lat_s) - 1, int(q * len(lat_s)))] if lat_s else None)
+    return {"served": st["cell_steps"] / wall / 1e9, "offered": offered / wall / 1e9,
+            "latency_s": {"p50": pct(0.5), "p99": pct(0.99), "completed": len(lat)},
+            "requests": {"arrived": pending, "completed": st["done"], "active_at_end": st["active"],
+                         "queued_at_end": st["queued"]},
+            "hbm": {"budget_bytes": budget, "peak_bytes_in_use": st["peak_bytes"],
+                    "mean_occupancy": (sum(occ) / len(occ) / budget) if occ else 0.0},
+            "launch_form": {"persistent": st["persistent"], "graph_captures": st["graph_captures"],
+                            "in_place_table_updates": st["table_updates"], "launches_per_step": st["launches_per_step"],
+                            "membership_changes": st["rebuilds"]}}
+
+
 def run_serve(args):
     """Serving workload: Poisson arrivals (mean --rate per second) of
     batch-like scenes with step counts log-uniform 200..8000, served by the
     continuous-batching loop under an HBM budget for --duration seconds of
-    wall clock; latency = completion - arrival.  Beside it, the plain path
-    solving a sample of the same requests one at a time (create + steps)."""
+    wall clock.  When that stream is more than the GPU sustains, the served
+    throughput is the server's capacity; capacity / mean work per request is
+    the highest sustainable arrival rate, and a second leg at 80 % of it
+    (--sustain-duration seconds) reports the latency of a stream the server
+    keeps up with.  Beside them, the plain path solving a sample of the same
+    requests one at a time (create + steps)."""
     import torch
     from openpstd_gb300 import build as _b, scenes
     from openpstd_gb300 import kernel
-    from openpstd_gb300.serving import Server
     _b.build()
     torch.cuda.set_device(0)
-    reqs = scenes.serving_requests(0, rate_hz=args.rate, duration_s=args.duration)
     budget = int(args.budget_gb * (1 << 30))
-    srv = Server(budget, max_scenes=4096)
-    pending, live = 0, {}
-    lat, occ = [], []
-    t0 = time.perf_counter()
+    reqs = scenes.serving_requests(0, rate_hz=args.rate, duration_s=args.duration)
     with ClockSampler(0) as clk:
-        while True:
-            now = time.perf_counter() - t0
-            if now >= args.duration:
-                break
-            while pending < len(reqs) and reqs[pending][0] <= now:
-                at, conf = reqs[pending]
-                rid = srv.submit(conf, conf.Settings.framecount())
-                live[rid] = at
-                pending += 1
-            info = srv.tick(args.tick_steps)
-            occ.append(srv.stats()["bytes_in_use"])
-            if info["finished"]:
-                t_done = time.perf_counter() - t0
-                for rid in list(live):
-                    if srv.poll(rid)["state"] == 2:
-                        lat.append(t_done - live.pop(rid))
-                        srv.result(rid)
-            if info["active"] == 0 and info["queued"] == 0 and pending < len(reqs):
-                time.sleep(max(0.0, min(reqs[pending][0] - (time.perf_counter() - t0), 0.01)))
-    wall = time.perf_counter() - t0
-    st = srv.stats()
-    srv.close()
-    served = st["cell_steps"] / wall / 1e9
+        main = serve_leg(reqs, args.duration, budget, args.tick_steps)
+    # mean work of a request of this mix (cell-steps), from a large sample of the generator
+    sample = scenes.serving_requests(7, rate_hz=100.0, duration_s=20.0)
+    mean_work = sum(request_cells(c) * c.Settings.framecount() for _, c in sample) / len(sample)
+    saturated = main["offered"] > 1.05 * main["served"]
+    sustain = None
+    if saturated and args.sustain_duration > 0:
+        r_max = main["served"] * 1e9 / mean_work
+        r = 0.8 * r_max
+        leg = serve_leg(scenes.serving_requests(1, rate_hz=r, duration_s=args.sustain_duration),
+                        args.sustain_duration, budget, args.tick_steps)
+        sustain = {"max_sustainable_rate_hz": r_max, "rate_hz": r, **leg}
     # plain path, one request at a time (create + all its steps), on a sample
     t_plain, cs_plain, n_plain = 0.0, 0, 0
     for at, conf in reqs[: args.plain_requests]:
@@ -404,8 +468,7 @@ def run_serve(args):
         if t_plain > args.plain_seconds:
             break
     plain = cs_plain / t_plain / 1e9
-    lat_s = sorted(lat)
-    pct = (lambda q: lat_s[min(len(lat_s) - 1, int(q * len(lat_s)))] if lat_s else None)
+    served = main["served"]
     line = {"metric": METRIC, "value": served, "unit": METRIC, "n_gpus": 1, "steps": None, "warmup": 0,
             "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded Poisson request stream)",
@@ -413,12 +476,10 @@ def run_serve(args):
                                    "1-6 rectangles), steps log-uniform 200..8000, HBM budget "
                                    f"{args.budget_gb} GB, {args.duration} s wall clock",
                        "tick_steps": args.tick_steps},
-            "latency_s": {"p50": pct(0.5), "p99": pct(0.99), "completed": len(lat)},
-            "requests": {"arrived": pending, "completed": st["done"], "active_at_end": st["active"],
-                         "queued_at_end": st["queued"]},
-            "hbm": {"budget_bytes": budget, "peak_bytes_in_use": st["peak_bytes"],
-                    "mean_occupancy": (sum(occ) / len(occ) / budget) if occ else 0.0},
-            "plan_rebuilds": st["rebuilds"],
+            "offered": main["offered"], "saturated": saturated,
+            "latency_s": main["latency_s"], "requests": main["requests"], "hbm": main["hbm"],
+            "launch_form": main["launch_form"], "mean_request_cell_steps": mean_work,
+            "sustained": sustain,
             "plain_serial": {"value": plain, "unit": METRIC, "requests": n_plain,
                              "note": "the first requests solved one at a time with the plain path (create + steps)"},
             "served_over_plain": served / plain if plain else None, "clocks": clk.summary()}
@@ -617,6 +678,8 @@ def main():
     ap.add_argument("--duration", type=float, default=60.0, help="serve: seconds of wall clock")
     ap.add_argument("--budget-gb", type=float, default=80.0, help="serve: HBM budget")
     ap.add_argument("--tick-steps", type=int, default=64, help="serve: most steps per tick")
+    ap.add_argument("--sustain-duration", type=float, default=60.0,
+                    help="serve: seconds of the leg at 80 %% of the highest sustainable rate (0: skip)")
     ap.add_argument("--plain-requests", type=int, default=40)
     ap.add_argument("--plain-seconds", type=float, default=20.0)
     args = ap.parse_args()

@@ -269,6 +269,11 @@ int pstd_server_cancel(pstd_server* s, int64_t request_id);
 /* stats[8] = {budget bytes, bytes in use, peak bytes in use, cell-steps done,
  *             requests done, plan rebuilds, active, queued} */
 int pstd_server_stats(pstd_server* s, int64_t* stats);
+/* launch form: out[4] = {CUDA graph captures, in-place table updates (membership
+ * changes served without a capture), 1 if the current step is the persistent
+ * form (one merged launch per RK stage, counts read from device memory),
+ * kernel launches per step} */
+int pstd_server_launch_stats(pstd_server* s, int64_t* out);
 
 /* ---- allocation-free solve (no counterpart in the reference) ------------
  * For callers that cannot allocate device memory: host applications that

@@ -117,11 +117,26 @@ inline int fp32_variants(const StageVariant* vs, int nv) {
 }
 
 // PSTD_PLAN="L:i,L:i,..." pins the variant of each listed strip length (for
-// profiling a plan the autotuner chose without a profiler); -1 = not listed
+// profiling a plan the autotuner chose without a profiler); -1 = not listed.
+// PSTD_PLAN=serving pins every length to the plain variant with the
+// configuration of the serving loop's per-length persistent form.
 inline int planned_variant(int L) {
     const char* e = std::getenv("PSTD_PLAN");
     if (!e) return -1;
     std::string s(e);
+    if (s == "serving") {
+        const StageVariant* sv = serve_variant(L);
+        const StageVariant* vs;
+        const int nv = stage_variants(L, &vs);
+        for (int i = 0; sv && i < nv; i++) {
+            const StageVariant& v = vs[i];
+            if (v.CS == sv->CS && v.NT == sv->NT && v.smem == sv->smem && v.ctw == sv->ctw && v.shf == 0 &&
+                !v.persistent && !v.pipe && !v.bf16 && !v.tma && !v.tc5 && v.r[0] == sv->r[0] && v.r[1] == sv->r[1] &&
+                v.r[2] == sv->r[2] && v.r[3] == sv->r[3])
+                return i;
+        }
+        return -1;
+    }
     size_t at = 0;
     while (at < s.size()) {
         size_t end = s.find(',', at);
@@ -140,6 +155,7 @@ inline int planned_variant(int L) {
 struct PlanChoice {
     std::vector<std::pair<int, const StageVariant*>> vars;   // (L, variant)
     bool merged = false;
+    int merged_fam = 0;
     bool longest_first = false;
     std::string form;
 };
@@ -242,6 +258,7 @@ struct Kernel {
         const DevSrvReceiver* rec = nullptr;
         float* aux = nullptr;
         int* scene_step = nullptr;
+        const int* limit = nullptr;   // per slot: the scene's step count
         const int* slots = nullptr;
         int n_slots = 0;
     } srv;
@@ -455,8 +472,35 @@ struct Kernel {
         std::vector<int> pml_idx;
         size_t set_floats = 0, fixed_floats = 0, p0_floats = 0;
     };
-    FieldLayout layout_fields() const {
+    // Offsets, pitches and constants of one domain in the layout of
+    // device.cuh.  off / foff / poff: the next free float of the state set,
+    // the fixed buffer and the p0 array (advanced past the domain); the
+    // attenuation offsets are left at -1 for the caller.
+    static void layout_domain(const Domain& d, const Scene& sc, int scene, long long& off, long long& foff,
+                              long long& poff, DevDomain& h) {
         auto round32 = [](long long v) { return (v + 31) / 32 * 32; };
+        std::memset(&h, 0, sizeof h);
+        h.nx = d.nx; h.ny = d.ny;
+        h.pitch_p = (int)round32(d.nx);
+        h.pitch_vx = (int)round32(d.nx + 1);
+        h.pitch_vy = (int)round32(d.nx);
+        h.fixed = d.rigid;
+        h.scene = scene;
+        long long& o = d.rigid ? foff : off;
+        h.o_px = o; o = round32(o + (long long)h.pitch_p * d.ny);
+        h.o_py = o; o = round32(o + (long long)h.pitch_p * d.ny);
+        h.o_vx = o; o = round32(o + (long long)h.pitch_vx * d.ny);
+        h.o_vy = o; o = round32(o + (long long)h.pitch_vy * (d.ny + 1));
+        h.o_p0 = poff; poff = round32(poff + (long long)h.pitch_p * d.ny);
+        h.rho = d.rho;
+        h.c2 = sc.s.c1 * sc.s.c1;
+        const float dt = sc.s.dt();
+        for (int i = 0; i < 6; i++) h.cdt[i] = dt * sc.s.rk[i];
+        h.pml = d.pml;
+        h.att_xp = h.att_xv = h.att_yp = h.att_yv = -1;
+    }
+
+    FieldLayout layout_fields() const {
         long long off = 0, foff = 0, poff = 0;
         FieldLayout out;
         out.doms.resize(gdom.size());
@@ -464,25 +508,7 @@ struct Kernel {
             const Domain& d = dom((int)k);
             const Scene& sc = scene_of((int)k);
             DevDomain& h = out.doms[k];
-            std::memset(&h, 0, sizeof h);
-            h.nx = d.nx; h.ny = d.ny;
-            h.pitch_p = (int)round32(d.nx);
-            h.pitch_vx = (int)round32(d.nx + 1);
-            h.pitch_vy = (int)round32(d.nx);
-            h.fixed = d.rigid;
-            h.scene = gdom[k].first;
-            long long& o = d.rigid ? foff : off;
-            h.o_px = o; o = round32(o + (long long)h.pitch_p * d.ny);
-            h.o_py = o; o = round32(o + (long long)h.pitch_p * d.ny);
-            h.o_vx = o; o = round32(o + (long long)h.pitch_vx * d.ny);
-            h.o_vy = o; o = round32(o + (long long)h.pitch_vy * (d.ny + 1));
-            h.o_p0 = poff; poff = round32(poff + (long long)h.pitch_p * d.ny);
-            h.rho = d.rho;
-            h.c2 = sc.s.c1 * sc.s.c1;
-            const float dt = sc.s.dt();
-            for (int i = 0; i < 6; i++) h.cdt[i] = dt * sc.s.rk[i];
-            h.pml = d.pml;
-            h.att_xp = h.att_xv = h.att_yp = h.att_yv = -1;
+            layout_domain(d, sc, gdom[k].first, off, foff, poff, h);
             if (d.pml) {
                 out.pml_idx.push_back((int)k);
                 std::vector<double> prof;
@@ -649,6 +675,7 @@ struct Kernel {
             plan(false);
             longest_first = cached.longest_first;
             if (cached.merged) {
+                merged_fam = cached.merged_fam;
                 build_merged();
                 merged = true;
                 capture_graphs();
@@ -667,6 +694,7 @@ struct Kernel {
                 for (auto& b : buckets) pc.vars.push_back({b.L, b.var});
                 pc.longest_first = longest_first;
                 pc.merged = merged;
+                pc.merged_fam = merged_fam;
                 pc.form = form_choice;
                 std::lock_guard<std::mutex> lock(plan_cache_mutex());
                 plan_cache()[sig] = pc;
@@ -703,6 +731,10 @@ struct Kernel {
         a.set_in = k == 0 ? c : ((k - 1) % 2 == 0 ? A : B);
         a.set_prev = c;
         a.err = derr.p;
+        if (dev_counts) {
+            a.scene_step = srv.scene_step;
+            a.scene_limit = srv.limit;
+        }
         return a;
     }
 
@@ -878,7 +910,7 @@ struct Kernel {
         steps = 0;
     }
 
-    int launches_per_step() const { return 6 * (int)stage_launches().size() + (n_pml > 0) + 1; }
+    int launches_per_step() const { return 6 * (int)stage_launches().size() + (n_pml > 0 || dev_counts) + 1; }
 
     // ---------------------------------------------------------------- merged form
     // One persistent launch per RK stage over the jobs of every length the
@@ -889,20 +921,45 @@ struct Kernel {
         const DevJob* jobs;
         int n, tw_off, fp, fv, rc;
         bool all;
+        const int* cnt = nullptr;   // device-count persistent launch (launch_dev): its job count
+        int ctr = 0;                // and its job counter (counters[stage * 16 + ctr])
     };
+    // serving form, one persistent launch per strip length: the configuration,
+    // first job in djobs_all, index of the job count in dev_counts, twiddles
+    struct DevRegion {
+        const StageVariant* var;
+        size_t base;
+        int count_idx;
+        int tw_off;
+    };
+    std::vector<DevRegion> dev_regions;
     struct SepBucket { int b, off, n; };
     bool merged = false;
+    int merged_fam = merged_family_default();   // configuration family of the merged launch
     bool longest_first = false;   // launch order of the lengths in a stage (buckets ascend in L)
     DevBuf<DevJob> djobs_all, djobs_sep;
     int n_all = 0;
     std::vector<SepBucket> sep;
     DevBuf<int> counters;
     std::string form_choice;
+    // serving form: counts in device memory, read by the launches themselves
+    // ({long jobs, short jobs, offset of the short-job table, PML domains, PML
+    // blocks, receivers, slots}); the tables behind them change in place
+    // between steps
+    const int* dev_counts = nullptr;
 
     std::vector<StageLaunch> stage_launches() const {
         std::vector<StageLaunch> v;
-        if (merged) {
-            if (n_all > 0) v.push_back({nullptr, djobs_all.p, n_all, 0, 0, 0, 0, true});
+        if (dev_counts && !dev_regions.empty()) {
+            for (size_t r = 0; r < dev_regions.size(); r++) {
+                const DevRegion& g = dev_regions[r];
+                StageLaunch l{g.var, djobs_all.p + g.base, 0, g.tw_off, 0, 0, 0, false};
+                l.cnt = dev_counts + g.count_idx;
+                l.ctr = (int)r;
+                v.push_back(l);
+            }
+        } else if (merged) {
+            if (n_all > 0 || dev_counts) v.push_back({nullptr, djobs_all.p, n_all, 0, 0, 0, 0, true});
             for (const SepBucket& q : sep) {
                 const Bucket& b = buckets[q.b];
                 v.push_back({b.var, djobs_sep.p + q.off, q.n, b.tw_off, b.fp_off, b.fv_off, b.rc, false});
@@ -931,7 +988,7 @@ struct Kernel {
         for (int i : order) {
             const Bucket& b = buckets[i];
             if (merged_supports(b.L) && !b.pinned) {
-                auto js = make_jobs(b.L, merged_variant(b.L), false);
+                auto js = make_jobs(b.L, merged_variant(b.L, merged_fam), false);
                 all.insert(all.end(), js.begin(), js.end());
             } else {
                 auto js = make_jobs(b.L, b.var, false);
@@ -939,13 +996,13 @@ struct Kernel {
                 rest.insert(rest.end(), js.begin(), js.end());
             }
         }
-        auto copies = make_jobs(-1, merged_variant(128), true);   // no strips of length -1: the copy jobs only
+        auto copies = make_jobs(-1, merged_variant(128, merged_fam), true);   // no strips of length -1: the copy jobs only
         all.insert(all.end(), copies.begin(), copies.end());
         n_all = (int)all.size();
         djobs_all.upload(all);
         djobs_sep.upload(rest);
         counters.alloc(6);
-        CK(prepare_stage_all());
+        CK(prepare_stage_all(merged_fam));
         upload_tables();
         while (side.size() < sep.size() + 1) {
             cudaStream_t st;
@@ -1037,26 +1094,44 @@ struct Kernel {
             build_merged();
             merged = true;
             capture_graphs();
-            form_choice = "merged launch (forced)";
+            form_choice = "merged launch (forced), family " + std::to_string(merged_fam);
             return;
         }
         merged = false;
         capture_graphs();
         const float t_len = time_steps(5);
         reset();
-        build_merged();
-        merged = true;
-        capture_graphs();
-        const float t_all = time_steps(5);
-        reset();
-        char buf[160];
-        std::snprintf(buf, sizeof buf, " (step %.1f us merged vs %.1f us per length)", t_all * 1e3f, t_len * 1e3f);
+        // both configuration families of the merged launch (PSTD_MERGED_FAMILY: that one only)
+        std::vector<int> fams{0, 1};
+        if (std::getenv("PSTD_MERGED_FAMILY")) fams.assign(1, merged_family_default());
+        float t_all = 1e30f;
+        int best_fam = fams[0];
+        std::string rec;
+        for (int f : fams) {
+            merged_fam = f;
+            build_merged();
+            merged = true;
+            capture_graphs();
+            const float t = time_steps(5);
+            reset();
+            char b[64];
+            std::snprintf(b, sizeof b, "%s%.1f us family %d", rec.empty() ? "" : ", ", t * 1e3f, f);
+            rec += b;
+            if (t < t_all) { t_all = t; best_fam = f; }
+        }
+        char buf[200];
+        std::snprintf(buf, sizeof buf, " (step merged %s vs %.1f us per length)", rec.c_str(), t_len * 1e3f);
         if (t_all >= t_len) {
             merged = false;
             capture_graphs();
             form_choice = std::string("per-length launches") + buf;
         } else {
-            form_choice = std::string("merged launch") + buf;
+            if (merged_fam != best_fam) {
+                merged_fam = best_fam;
+                build_merged();
+                capture_graphs();
+            }
+            form_choice = std::string("merged launch, family ") + std::to_string(best_fam) + buf;
         }
     }
 
@@ -1073,7 +1148,7 @@ struct Kernel {
             tmp.push_back(e);
             return e;
         };
-        if (merged) CK(cudaMemsetAsync(counters.p, 0, 6 * sizeof(int), st));   // per-stage job counters
+        if (merged) CK(cudaMemsetAsync(counters.p, 0, counters.n * sizeof(int), st));   // per-stage job counters
         for (int k = 0; k < 6; k++) {
             cudaEvent_t t0 = nullptr, t1 = nullptr;
             if (ev) {
@@ -1083,8 +1158,14 @@ struct Kernel {
             }
             const std::vector<StageLaunch> ls = stage_launches();
             auto launch = [&](const StageLaunch& l, cudaStream_t s) {
-                if (l.all) {
-                    CK(launch_stage_all(l.n, stage_args(c, k, l.jobs, dtw.p, 0, 0, 0), counters.p + k, s));
+                if (l.cnt) {
+                    StageArgs a = stage_args(c, k, l.jobs, dtw.p + l.tw_off, 0, 0, 0);
+                    CK(l.var->launch_dev(l.cnt, a, counters.p + k * 16 + l.ctr, s));
+                } else if (l.all && dev_counts) {
+                    CK(launch_stage_all_dev(merged_fam, dev_counts, stage_args(c, k, l.jobs, dtw.p, 0, 0, 0),
+                                            counters.p + k, s));
+                } else if (l.all) {
+                    CK(launch_stage_all(merged_fam, l.n, stage_args(c, k, l.jobs, dtw.p, 0, 0, 0), counters.p + k, s));
                 } else {
                     StageArgs a = stage_args(c, k, l.jobs, dtw.p + l.tw_off, l.fp, l.fv, l.rc);
                     CK(l.var->launch(l.n, a, s));
@@ -1113,12 +1194,15 @@ struct Kernel {
                 ev->push_back({t0, t1});
             }
         }
-        if (n_pml > 0)
+        if (dev_counts)
+            CK(launch_pml_post_dev(dpml.p, dev_counts + 3, dpml_off.p, ddoms.p, sets[B].p, fixed.p, p0.p, datt.p,
+                                   srv.scene_step, srv.limit, st));
+        else if (n_pml > 0)
             CK(launch_pml_post(dpml.p, n_pml, pml_blocks, ddoms.p, sets[B].p, fixed.p, p0.p, datt.p, st, dpml_off.p));
         if (srv.on) {
             CK(cudaMemsetAsync(first_step.p, 0, srv.n_flags * sizeof(int), st));
-            CK(launch_server_receivers(srv.rec, n_rec, ddoms.p, sets[B].p, srv.aux, srv.scene_step, srv.slots,
-                                       srv.n_slots, st));
+            CK(launch_server_receivers(srv.rec, n_rec, ddoms.p, sets[B].p, srv.aux, srv.scene_step, srv.limit,
+                                       srv.slots, srv.n_slots, st, dev_counts ? dev_counts + 5 : nullptr));
         } else {
             CK(cudaMemsetAsync(first_step.p, 0, scenes.size() * sizeof(int), st));
             CK(launch_receivers(drec.p, n_rec, ddoms.p, sets[B].p, dring.p, ring_cap, dcounter.p, st));

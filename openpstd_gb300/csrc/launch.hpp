@@ -32,6 +32,10 @@ struct StageArgs {
     const unsigned char* maps;
     int set_in, set_prev;
     int* err;
+    // serving loop, persistent form: per-scene steps taken and step limits; a
+    // job of a scene that has taken all its steps is skipped (null: none skip)
+    const int* scene_step = nullptr;
+    const int* scene_limit = nullptr;
 };
 
 constexpr int PSTD_TMAP_BYTES = 128;   // sizeof(CUtensorMap)
@@ -62,6 +66,12 @@ struct StageVariant {
     cudaError_t (*prepare)();
     size_t (*smem_for)(int row_cap);                            // dynamic shared memory of one CTA
     const char* name;
+    // persistent form over a job table whose length is read from device
+    // memory at launch time (serving loop; null where not compiled): resident
+    // CTAs take jobs from *counter, skip all-zero jobs and jobs of scenes at
+    // their step limit
+    cudaError_t (*launch_dev)(const int* count, const StageArgs& a, int* counter, cudaStream_t st) = nullptr;
+    cudaError_t (*prepare_dev)() = nullptr;
 };
 
 // all variants compiled for length L (nullptr / 0 if L is not supported)
@@ -71,23 +81,45 @@ int stage_variants(int L, const StageVariant** out);
 // of every length 128..2048; CTAs take jobs from *counter (zeroed before the
 // stage); jobs carry their own length and twiddle-table offset
 bool merged_supports(int L);
-const StageVariant* merged_variant(int L);
-cudaError_t prepare_stage_all();
-cudaError_t launch_stage_all(int n_jobs, const StageArgs& a, int* counter, cudaStream_t st);
+// configuration family fam: 0 = 256 threads, 3 CTAs per SM; 1 = 128 threads,
+// 8 CTAs per SM, computed twiddles (PSTD_MERGED_FAMILY picks the default)
+int merged_family_default();
+const StageVariant* merged_variant(int L, int fam);
+cudaError_t prepare_stage_all(int fam);
+cudaError_t launch_stage_all(int fam, int n_jobs, const StageArgs& a, int* counter, cudaStream_t st);
+// the same over two job tables in one array, counts read from device memory
+// at launch time: counts[0] jobs at a.jobs[0..), then counts[1] jobs at
+// a.jobs[counts[2]..) (all resident CTAs start; zero counts are an empty
+// stage).  All-zero jobs (length 0, no copy flag) are skipped.
+cudaError_t launch_stage_all_dev(int fam, const int* counts, const StageArgs& a, int* counter, cudaStream_t st);
+
+// serving loop, per-length persistent form (stage_serve.cu): one compiled
+// configuration per transform length 32..8192 with launch_dev set (nullptr
+// for other lengths)
+const StageVariant* serve_variant(int L);
 
 // one block per (row, 128-column chunk): with off (n + 1 prefix sums of the
 // domains' (rows + 1) x ceil((columns + 1) / 128) block counts) blocks is their
 // total; without, blocks is the count of the largest domain (grid blocks x n)
 cudaError_t launch_pml_post(const int* doms_idx, int n, int blocks, const DevDomain* doms, float* set, float* fixed,
                             float* p0, const float* att, cudaStream_t st, const int* off = nullptr);
+// the same with n and blocks read from device memory (counts[0], counts[1]) by a
+// fixed grid that strides over the blocks; domains of scenes that have taken
+// all their steps (scene_step >= scene_limit) are left alone
+cudaError_t launch_pml_post_dev(const int* doms_idx, const int* counts, const int* off, const DevDomain* doms,
+                                float* set, float* fixed, float* p0, const float* att, const int* scene_step,
+                                const int* scene_limit, cudaStream_t st);
 cudaError_t launch_speakers(const DevDomain* doms, const int* x0, const int* y0, int n_dom, const DevSpeaker* spk,
                             int n_spk, float dx, float bw, float* set, float* fixed, float* p0, cudaStream_t st);
 cudaError_t launch_receivers(const DevReceiver* rec, int n_rec, const DevDomain* doms, const float* set, float* ring,
                              int cap, int* counter, cudaStream_t st);
 // serving loop: one sample per receiver into its scene's ring at the scene's
-// step count, then every listed slot's step count + 1
+// step count, then every listed slot's step count + 1 -- only for scenes below
+// their step limit (counts: n_rec and n_slots read from device memory,
+// counts[0] and counts[1])
 cudaError_t launch_server_receivers(const DevSrvReceiver* rec, int n_rec, const DevDomain* doms, const float* set,
-                                    float* aux, int* scene_step, const int* slots, int n_slots, cudaStream_t st);
+                                    float* aux, int* scene_step, const int* scene_limit, const int* slots, int n_slots,
+                                    cudaStream_t st, const int* counts = nullptr);
 // dense p0 = px + py of the given domains into dst (frames); sub > 1 keeps
 // every sub-th row and column (ceil(nx/sub) x ceil(ny/sub) values per domain);
 // n_rec floats of rec_src (a receiver row) are copied to rec_dst on the way

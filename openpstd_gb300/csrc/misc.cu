@@ -70,22 +70,9 @@ int stage_variants(int L, const StageVariant** out) {
 // (the reference does not recompute p0 after it), then px *= ax, py *= ay.
 // vx and vy of non-rigid domains were attenuated in the stage epilogue; rigid
 // domains (fields in the fixed buffer) get all four multiplies here.
-__global__ void pml_post_kernel(const int* idx, int n, const int* off, const DevDomain* doms, float* set,
-                                float* fixed, float* p0, const float* __restrict__ att) {
-    // one element per thread, one block per (row, 128-column chunk) of a domain.
-    // off (prefix sums of the domains' block counts): a flat grid, the block's
-    // domain found by binary search; off == nullptr: domain = blockIdx.y.
-    int dj = blockIdx.y, lb = blockIdx.x;
-    if (off) {
-        int lo = 0, hi = n - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (off[mid] <= (int)blockIdx.x) lo = mid;
-            else hi = mid - 1;
-        }
-        dj = lo;
-        lb = blockIdx.x - off[lo];
-    }
+// one (row, 128-column chunk) block `lb` of PML domain doms[idx[dj]]
+__device__ __forceinline__ void pml_post_block(int dj, int lb, const int* idx, const DevDomain* doms, float* set,
+                                               float* fixed, float* p0, const float* __restrict__ att) {
     const DevDomain d = doms[idx[dj]];
     float* base = d.fixed ? fixed : set;
     const int chunks = (d.nx + 1 + 127) >> 7;   // vx rows have nx + 1 columns
@@ -106,6 +93,44 @@ __global__ void pml_post_kernel(const int* idx, int n, const int* off, const Dev
             const long long e = d.o_vy + (long long)r * d.pitch_vy + i;
             base[e] = __fmul_rn(base[e], att[d.att_yv + r]);
         }
+    }
+}
+
+// the domain of flat block b: the last k with off[k] <= b (off ascends, off[0] = 0)
+__device__ __forceinline__ int pml_domain_of(const int* off, int n, int b) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (off[mid] <= b) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void pml_post_kernel(const int* idx, int n, const int* off, const DevDomain* doms, float* set,
+                                float* fixed, float* p0, const float* __restrict__ att) {
+    // one element per thread, one block per (row, 128-column chunk) of a domain.
+    // off (prefix sums of the domains' block counts): a flat grid, the block's
+    // domain found by binary search; off == nullptr: domain = blockIdx.y.
+    int dj = blockIdx.y, lb = blockIdx.x;
+    if (off) {
+        dj = pml_domain_of(off, n, (int)blockIdx.x);
+        lb = blockIdx.x - off[dj];
+    }
+    pml_post_block(dj, lb, idx, doms, set, fixed, p0, att);
+}
+
+// the flat form with the domain and block counts in device memory: a fixed
+// grid strides over the blocks
+__global__ void pml_post_dev_kernel(const int* idx, const int* counts, const int* off, const DevDomain* doms,
+                                    float* set, float* fixed, float* p0, const float* __restrict__ att,
+                                    const int* scene_step, const int* scene_limit) {
+    const int n = counts[0], blocks = counts[1];
+    for (int b = blockIdx.x; b < blocks; b += gridDim.x) {
+        const int dj = pml_domain_of(off, n, b);
+        const int sc = doms[idx[dj]].scene;
+        if (scene_step[sc] >= scene_limit[sc]) continue;   // the same for the whole block
+        pml_post_block(dj, b - off[dj], idx, doms, set, fixed, p0, att);
     }
 }
 
@@ -158,17 +183,23 @@ __global__ void receiver_kernel(const DevReceiver* rec, int n_rec, const DevDoma
 }
 
 __global__ void server_receiver_kernel(const DevSrvReceiver* rec, int n_rec, const DevDomain* doms,
-                                       const float* __restrict__ set, float* aux, int* scene_step, const int* slots,
-                                       int n_slots) {
+                                       const float* __restrict__ set, float* aux, int* scene_step,
+                                       const int* scene_limit, const int* slots, int n_slots, const int* counts) {
+    if (counts) {
+        n_rec = counts[0];
+        n_slots = counts[1];
+    }
     for (int r = threadIdx.x; r < n_rec; r += blockDim.x) {
         const DevSrvReceiver q = rec[r];
+        const long long step = scene_step[q.slot];
+        if (step >= scene_limit[q.slot]) continue;   // the ring holds exactly the scene's steps
         const DevDomain d = doms[q.dom];
         const long long e = (long long)q.row * d.pitch_p + q.col;
-        const long long step = scene_step[q.slot];
         aux[q.ring + step * q.stride + q.index] = __fadd_rn(set[d.o_px + e], set[d.o_py + e]);
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < n_slots; i += blockDim.x) scene_step[slots[i]] += 1;
+    for (int i = threadIdx.x; i < n_slots; i += blockDim.x)
+        if (scene_step[slots[i]] < scene_limit[slots[i]]) scene_step[slots[i]] += 1;
 }
 
 // p0 = px + py of every `sub`-th row and column (sub = 1: the whole domain)
@@ -196,6 +227,20 @@ cudaError_t launch_pml_post(const int* idx, int n, int blocks, const DevDomain* 
     return cudaGetLastError();
 }
 
+cudaError_t launch_pml_post_dev(const int* idx, const int* counts, const int* off, const DevDomain* doms, float* set,
+                                float* fixed, float* p0, const float* att, const int* scene_step,
+                                const int* scene_limit, cudaStream_t st) {
+    static int grid = 0;
+    if (grid == 0) {
+        int dev, sms;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        grid = sms * 16;   // 16 blocks of 128 threads per SM
+    }
+    pml_post_dev_kernel<<<grid, 128, 0, st>>>(idx, counts, off, doms, set, fixed, p0, att, scene_step, scene_limit);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_speakers(const DevDomain* doms, const int* x0, const int* y0, int n_dom, const DevSpeaker* spk,
                             int n_spk, float dx, float bw, float* set, float* fixed, float* p0, cudaStream_t st) {
     if (n_dom <= 0) return cudaSuccess;
@@ -210,9 +255,11 @@ cudaError_t launch_receivers(const DevReceiver* rec, int n_rec, const DevDomain*
 }
 
 cudaError_t launch_server_receivers(const DevSrvReceiver* rec, int n_rec, const DevDomain* doms, const float* set,
-                                    float* aux, int* scene_step, const int* slots, int n_slots, cudaStream_t st) {
-    if (n_slots <= 0) return cudaSuccess;
-    server_receiver_kernel<<<1, 256, 0, st>>>(rec, n_rec, doms, set, aux, scene_step, slots, n_slots);
+                                    float* aux, int* scene_step, const int* scene_limit, const int* slots,
+                                    int n_slots, cudaStream_t st, const int* counts) {
+    if (n_slots <= 0 && !counts) return cudaSuccess;
+    server_receiver_kernel<<<1, 256, 0, st>>>(rec, n_rec, doms, set, aux, scene_step, scene_limit, slots, n_slots,
+                                              counts);
     return cudaGetLastError();
 }
 

@@ -1378,6 +1378,43 @@ __global__ void __launch_bounds__(C::NT, C::MINB) stage_kernel(StageArgs A) {
     epilogue<C, C::NT>(sm, A, job, dom, threadIdx.x);
 }
 
+// The plain stage kernel as a persistent loop over a job table whose length
+// is read from device memory (serving loop): resident CTAs take jobs from
+// *counter; all-zero entries (free table ranges: length 0, no copy flag) and
+// jobs of scenes that have taken all their steps are skipped.
+template <class C>
+__global__ void __launch_bounds__(C::NT, C::MINB) stage_kernel_dev(const __grid_constant__ StageArgs A, const int* count,
+                                                                  int* counter) {
+    extern __shared__ __align__(16) float2 sm[];
+    __shared__ int s_job;
+    const int n = *count;
+    for (;;) {
+        if (threadIdx.x == 0) s_job = atomicAdd(counter, 1);
+        __syncthreads();
+        const int j = s_job;
+        if (j >= n) break;   // the same value for the whole CTA
+        const DevJob job = A.jobs[j];
+        const DevDomain dom = A.doms[job.dom];
+        const bool live = !A.scene_limit || A.scene_step[dom.scene] < A.scene_limit[dom.scene];
+        if (!live || (job.L == 0 && !(job.kind & JK_COPY))) {
+        } else if (job.kind & JK_COPY) {
+            copy_axis<C::NT>(A, dom, job.kind & JK_Y, threadIdx.x);
+        } else {
+            const bool first = A.first_step[dom.scene] != 0;
+            gather<C, C::NT, false>(sm, A, job, dom, first, threadIdx.x);
+            __syncthreads();
+            const bool vel = job.kind & JK_VEL;
+            const int nn = ((job.kind & JK_Y) ? dom.ny : dom.nx) + (vel ? 1 : 0);
+            const int nout = vel ? nn - 1 : nn + 1;
+            convolve<C, C::NT, 0, false, true>(sm, A.tw, A.filt + job.dtab, threadIdx.x, 2 * job.W + nn, job.W,
+                                               job.W + nout);
+            __syncthreads();
+            epilogue<C, C::NT>(sm, A, job, dom, threadIdx.x);
+        }
+        __syncthreads();   // shared memory and s_job are reused by the next job
+    }
+}
+
 // ---------------------------------------------------------------- persistent form
 // named barriers: 1,2 buffer full; 3,4 buffer transformed; 5 FFT warps; 6 memory warps
 template <class C>
@@ -1912,6 +1949,25 @@ cudaError_t prepare_stage_t() {
 }
 
 template <class C>
+cudaError_t launch_stage_dev_t(const int* count, const StageArgs& a, int* counter, cudaStream_t st) {
+    static int grid = 0;
+    if (grid == 0) {
+        int dev, sms, per = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, stage_kernel_dev<C>, C::NT, C::SMEM);
+        grid = sms * (per > 0 ? per : 1);
+    }
+    stage_kernel_dev<C><<<grid, C::NT, C::SMEM, st>>>(a, count, counter);
+    return cudaGetLastError();
+}
+
+template <class C>
+cudaError_t prepare_stage_dev_t() {
+    return cudaFuncSetAttribute(stage_kernel_dev<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM);
+}
+
+template <class C>
 StageVariant make_variant(const char* name) {
     StageVariant v;
     v.L = C::L; v.CS = C::CS; v.NT = C::NT + C::NTP; v.smem = C::SMEM; v.np = C::NP;
@@ -1924,6 +1980,16 @@ StageVariant make_variant(const char* name) {
     v.prepare = &prepare_stage_t<C>;
     v.smem_for = &plain_smem<C>;
     v.name = name;
+    return v;
+}
+
+// a plain variant that also has the device-count persistent form
+template <class C>
+StageVariant make_dev_variant(const char* name) {
+    static_assert(C::NTP == 0 && C::TC == 0, "the device-count form runs the plain stage kernel");
+    StageVariant v = make_variant<C>(name);
+    v.launch_dev = &launch_stage_dev_t<C>;
+    v.prepare_dev = &prepare_stage_dev_t<C>;
     return v;
 }
 

@@ -83,7 +83,11 @@ class Server:
         s = (ctypes.c_int64 * 8)()
         _lib.check(_lib.lib().pstd_server_stats(self._h, s))
         keys = ["budget_bytes", "bytes_in_use", "peak_bytes", "cell_steps", "done", "rebuilds", "active", "queued"]
-        return dict(zip(keys, list(s)))
+        out = dict(zip(keys, list(s)))
+        f = (ctypes.c_int64 * 4)()
+        _lib.check(_lib.lib().pstd_server_launch_stats(self._h, f))
+        out.update(graph_captures=f[0], table_updates=f[1], persistent=bool(f[2]), launches_per_step=f[3])
+        return out
 
     def run_until_idle(self, max_steps: int = 64, limit: Optional[int] = None) -> int:
         """Tick until nothing is queued or active; returns the number of ticks."""
