@@ -226,8 +226,20 @@ int pstd_profile_passes(pstd_kernel* k, int32_t n_steps, void* stream,
                         float* ms_stage, float* ms_total, int32_t* stage_launches, int32_t* total_launches);
 
 /* Stage-kernel plan: one line per strip-length bucket (length, jobs,
- * variant chosen by the autotuner and the timings it compared). */
+ * variant chosen by the autotuner with its index, the timings it compared). */
 int pstd_plan_info(pstd_kernel* k, char* buf, int32_t cap);
+
+/* The stage-kernel variants compiled for transform length L, one line per
+ * variant: "<index> <name>" (the index PSTD_PLAN=L:index pins).  Host only:
+ * no GPU needed.  *n (may be NULL) = number of variants. */
+int pstd_stage_variants(int32_t L, char* buf, int32_t cap, int32_t* n);
+
+/* The round-trip gain per frequency bin (natural order, k < L) of the stage
+ * kernel's transform with passes radices[0..np) (last pass in registers),
+ * computed twiddles (ctw) or the last radix split over a lane pair
+ * (lane_pair), from the rounding of its float constants; the derivative
+ * filters are divided by it.  out: 2 L doubles (re, im).  Host only. */
+int pstd_transform_gain(int32_t L, const int32_t* radices, int32_t np, int32_t ctw, int32_t lane_pair, double* out);
 
 /* Counts that define the work: cells advanced per step (pressure cells of
  * non-rigid domains), of which air cells, and the number of kernel launches

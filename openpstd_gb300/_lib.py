@@ -73,6 +73,8 @@ SIGNATURES = {
     "pstd_server_poll": (ctypes.c_int, [_vp, _i64, _P(_i32), _P(_i32), _P(_i64)]),
     "pstd_server_result": (ctypes.c_int, [_vp, _i64, _P(_f32), _i64, _P(_f32), _i64]),
     "pstd_server_cancel": (ctypes.c_int, [_vp, _i64]),
+    "pstd_stage_variants": (ctypes.c_int, [_i32, ctypes.c_char_p, _i32, _P(_i32)]),
+    "pstd_transform_gain": (ctypes.c_int, [_i32, _P(_i32), _i32, _i32, _i32, _P(ctypes.c_double)]),
     "pstd_server_stats": (ctypes.c_int, [_vp, _P(_i64)]),
     "pstd_server_launch_stats": (ctypes.c_int, [_vp, _P(_i64)]),
     "pstd_solve_noalloc": (ctypes.c_int, [_P(c_config), _i32, _vp, _i64, _vp, _i64, _vp]),

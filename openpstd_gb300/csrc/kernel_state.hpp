@@ -20,6 +20,7 @@
 #include <tuple>
 #include <vector>
 
+#include "transform_gain.hpp"
 #include "../../include/pstd_gb300.h"
 #include "launch.hpp"
 #include "scene.hpp"
@@ -114,6 +115,16 @@ inline int fp32_variants(const StageVariant* vs, int nv) {
     int n = 0;
     while (n < nv && !vs[n].bf16) n++;
     return n;
+}
+
+// PSTD_GAIN_COMPENSATION=0 builds the derivative filters without dividing by
+// the transform's round-trip gain (for measuring what the division buys)
+inline bool gain_compensation() {
+    static const bool on = [] {
+        const char* e = std::getenv("PSTD_GAIN_COMPENSATION");
+        return !e || std::atoi(e) != 0;
+    }();
+    return on;
 }
 
 // PSTD_PLAN="L:i,L:i,..." pins the variant of each listed strip length (for
@@ -231,7 +242,7 @@ struct Kernel {
     std::vector<float> win;
     std::map<std::pair<int, int>, int> win_off;   // (W, patch error)
     std::vector<float2> filt;
-    std::map<std::tuple<int, int, int, int, int, int, float>, int> filt_off;   // (L, vel, radices, dx)
+    std::map<std::tuple<int, int, int, int, int, int, float, int>, int> filt_off;   // (L, vel, radices, dx, form)
     std::vector<float2> tw;
     std::map<std::tuple<int, int, int, int, int, int>, int> tw_off;   // (L, radices, lane-pair split / computed twiddles)
 
@@ -293,11 +304,18 @@ struct Kernel {
         return o;
     }
 
+    // The derivative filter of a variant: the reference's factors, 1/L, and the
+    // division by the round-trip gain of the variant's transform per bin
+    // (transform_gain.hpp; the tensor-core study forms are left as they are).
     int filter_of(int L, bool vel, const StageVariant* v, float dxf) {
-        auto key = std::make_tuple(L, (int)vel, v->r[0], v->r[1], v->r[2], v->r[3], dxf);
+        const bool study = v->bf16 || v->tc5;
+        const int form = study ? 3 : (v->shf ? 2 : 0) + (v->ctw ? 1 : 0) * 4;
+        auto key = std::make_tuple(L, (int)vel, v->r[0], v->r[1], v->r[2], v->r[3], dxf, form);
         auto it = filt_off.find(key);
         if (it != filt_off.end()) return it->second;
         int o = (int)filt.size();
+        std::vector<std::complex<double>> gain(L, std::complex<double>(1, 0));
+        if (!study && gain_compensation()) gain = tgain::round_trip_gain(L, v->r, v->np, v->ctw != 0, v->shf != 0);
         // kernel/core/WisdomCache.cpp:53-75: k_j = j (pi/dx)/(L/2) for bins
         // 0..L/2, factor exp(-/+ i k dx/2) * i k; Hermitian extension; 1/L
         const double dx = (double)dxf;
@@ -313,7 +331,7 @@ struct Kernel {
         std::vector<int> pos = bin_positions(L, v->r, v->np);
         std::vector<float2> perm(L);
         for (int j = 0; j < L; j++) {
-            std::complex<double> c = full[j] / (double)L;
+            std::complex<double> c = full[j] / (double)L / gain[j];
             perm[pos[j]] = make_float2((float)c.real(), (float)c.imag());
         }
         filt.insert(filt.end(), perm.begin(), perm.end());

@@ -515,11 +515,48 @@ int pstd_work_counts(pstd_kernel* h, int64_t* cells, int64_t* air, int32_t* laun
     return PSTD_OK;
 }
 
+int pstd_stage_variants(int32_t L, char* buf, int32_t cap, int32_t* n) {
+    const StageVariant* vs;
+    const int nv = stage_variants(L, &vs);
+    if (n) *n = nv;
+    std::string s;
+    for (int i = 0; i < nv; i++) s += std::to_string(i) + " " + vs[i].name + "\n";
+    if (buf && cap > 0) {
+        std::strncpy(buf, s.c_str(), (size_t)cap - 1);
+        buf[cap - 1] = 0;
+    }
+    return PSTD_OK;
+}
+
+int pstd_transform_gain(int32_t L, const int32_t* radices, int32_t np, int32_t ctw, int32_t lane_pair, double* out) {
+    if (!radices || !out || np < 1 || np > 4 || L < 2) return fail(PSTD_ERR_INVALID, "bad transform description");
+    int r[4] = {0, 0, 0, 0}, prod = 1;
+    for (int p = 0; p < np; p++) {
+        r[p] = radices[p];
+        if (r[p] != 2 && r[p] != 4 && r[p] != 8 && r[p] != 16 && r[p] != 32 && !(lane_pair && p == np - 1 && r[p] == 64))
+            return fail(PSTD_ERR_INVALID, "radix must be 2, 4, 8, 16 or 32");
+        prod *= r[p];
+    }
+    if (prod != L) return fail(PSTD_ERR_INVALID, "radices do not multiply to L");
+    const std::vector<std::complex<double>> g = tgain::round_trip_gain(L, r, np, ctw != 0, lane_pair != 0);
+    for (int k = 0; k < L; k++) {
+        out[2 * k] = g[k].real();
+        out[2 * k + 1] = g[k].imag();
+    }
+    return PSTD_OK;
+}
+
 int pstd_plan_info(pstd_kernel* h, char* buf, int32_t cap) {
     NEED_DEVICE(h);
     std::string s;
-    for (auto& b : h->k->buckets)
-        s += "L=" + std::to_string(b.L) + " jobs=" + std::to_string(b.n) + " variant=" + b.var->name + b.choice + "\n";
+    for (auto& b : h->k->buckets) {
+        // the variant's index in the length's list (PSTD_PLAN=L:index pins it)
+        const StageVariant* vs;
+        const int nv = stage_variants(b.L, &vs);
+        const long idx = (nv > 0 && b.var >= vs && b.var < vs + nv) ? (long)(b.var - vs) : -1;
+        s += "L=" + std::to_string(b.L) + " jobs=" + std::to_string(b.n) + " variant[" + std::to_string(idx) +
+             "]=" + b.var->name + b.choice + "\n";
+    }
     if (!h->k->form_choice.empty()) s += "form: " + h->k->form_choice + "\n";
     if (h->k->longest_first) s += "order: longest transforms launched first\n";
     if (buf && cap > 0) {

@@ -45,6 +45,7 @@
 #include <cstdint>
 
 #include "launch.hpp"
+#include "transform_gain.hpp"
 
 namespace pstd {
 
@@ -62,10 +63,7 @@ __device__ __forceinline__ float2 rot(float2 a) {   // * -i (forward) or * +i (i
     return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
 }
 
-// cos / sin of multiples of pi/8
-#define PSTD_C8 0.92387953251128674f
-#define PSTD_S8 0.38268343236508978f
-#define PSTD_R2 0.70710678118654752f
+// cos / sin of multiples of pi/8 and pi/16: PSTD_C8 .. PSTD_S316 (transform_gain.hpp)
 
 template <int K, bool INV>
 __device__ __forceinline__ float2 tw16(float2 a) {   // a * exp(-/+ 2 pi i K / 16)
@@ -142,10 +140,6 @@ struct DFT<16, INV> {
 };
 
 // a * exp(-/+ 2 pi i K / 32); odd K use cos / sin of multiples of pi/16
-#define PSTD_C16 0.98078528040323044913f   // cos(pi/16)
-#define PSTD_S16 0.19509032201612826785f   // sin(pi/16)
-#define PSTD_C316 0.83146961230254523708f  // cos(3 pi/16)
-#define PSTD_S316 0.55557023301960222474f  // sin(3 pi/16)
 template <int K, bool INV>
 __device__ __forceinline__ float2 tw32(float2 a) {
     constexpr float sg = INV ? 1.f : -1.f;

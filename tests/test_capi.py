@@ -104,3 +104,38 @@ def test_configuration_mirror():
     conf = scenes.plain_square(0)
     assert conf.Settings.framecount() == 500
     assert scenes.l_shape(0).Settings.framecount() == 4000
+
+
+def test_stage_variant_list(pstd_lib):
+    """pstd_stage_variants: the compiled variants of a length as "<index> <name>"
+    lines (the indices PSTD_PLAN pins); host only."""
+    import ctypes
+    buf, n = ctypes.create_string_buffer(1 << 14), ctypes.c_int32()
+    assert pstd_lib.pstd_stage_variants(128, buf, 1 << 14, ctypes.byref(n)) == 0
+    lines = buf.value.decode().splitlines()
+    assert n.value == len(lines) > 0
+    for i, line in enumerate(lines):
+        idx, name = line.split(" ", 1)
+        assert int(idx) == i and name.startswith("L128 ")
+    assert pstd_lib.pstd_stage_variants(100, buf, 1 << 14, ctypes.byref(n)) == 0 and n.value == 0
+
+
+@pytest.mark.parametrize("L,radices,ctw,lane_pair", [
+    (128, (16, 8), 0, 0), (128, (16, 8), 1, 0), (512, (8, 8, 8), 1, 0), (1024, (32, 32), 0, 0),
+    (1024, (16, 8, 8), 0, 0), (256, (8, 32), 0, 1), (512, (16, 32), 1, 1)])
+def test_transform_gain_model(pstd_lib, L, radices, ctw, lane_pair):
+    """The per-bin round-trip gain the derivative filters are divided by
+    (first order in the float constants' rounding) against an exact emulation
+    of the transform's passes: equal to 1e-12; and the uncompensated gain is
+    biased (every plan loses amplitude on average)."""
+    import ctypes
+    import numpy as np
+    from transform_model import round_trip_gain
+    r = (ctypes.c_int32 * 4)(*radices)
+    out = np.zeros(2 * L)
+    assert pstd_lib.pstd_transform_gain(L, r, len(radices), ctw, lane_pair,
+                                        out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))) == 0
+    model = out[0::2] + 1j * out[1::2]
+    exact = round_trip_gain(L, radices, bool(ctw), bool(lane_pair))
+    assert np.abs(model - exact).max() < 1e-12, np.abs(model - exact).max()
+    assert (model - 1).real.mean() < -2e-8

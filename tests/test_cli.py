@@ -41,9 +41,11 @@ def test_cli_create_and_gpu_only(tmp_path):
 
 
 @pytest.mark.gpu
-def test_cli_run_gpu_and_device_subsampling(tmp_path):
+def test_cli_run_gpu_and_device_subsampling(tmp_path, monkeypatch):
     from openpstd_gb300 import scenes
     from openpstd_gb300.kernel import KernelCallback, PSTDKernel
+    # both processes run the same variants (each would autotune on its own)
+    monkeypatch.setenv("PSTD_VARIANT", "0")
     conf = scenes.plain_square(4, n=90, steps=12, pml=40)
     p = tmp_path / "scene.json"
     conf.save(str(p))

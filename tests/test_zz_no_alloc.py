@@ -27,10 +27,22 @@ def _configs():
 
 def _existing(conf, steps):
     """Frame (p0 of the non-PML domains, scene order) and receiver samples
-    after `steps` steps through pstd_create + pstd_advance."""
+    after `steps` steps through pstd_create + pstd_advance, with the variant
+    the allocation-free solve runs (each length's first one; PSTD_VARIANT=0):
+    variants differ in rounding, and each divides its filter by its own
+    transform's gain."""
+    import os
     from openpstd_gb300.kernel import PSTDKernel
-    k = PSTDKernel()
-    k.initialize_kernel(conf)
+    keep = os.environ.get("PSTD_VARIANT")
+    os.environ["PSTD_VARIANT"] = "0"
+    try:
+        k = PSTDKernel()
+        k.initialize_kernel(conf)
+    finally:
+        if keep is None:
+            del os.environ["PSTD_VARIANT"]
+        else:
+            os.environ["PSTD_VARIANT"] = keep
     k.advance(steps)
     k.synchronize()
     frame = [k.snapshot(i, "p0").ravel() for i in range(k.domain_count()) if not k.domain_info(i)["is_pml"]]
