@@ -11,17 +11,19 @@ PSTDKernel restated in its own precision) and the FP64 oracle run on:
   speakers.
 
 Tolerances (relative L2):
-* receiver series: <= 1e-5 against the FP64 oracle, or <= 5x the float
-  oracle's own distance to FP64 (+1e-6) where that distance is above 1e-5/5;
-  and <= 1e-5 against the float oracle wherever the float oracle is within
-  1e-5/5 of FP64;
-* final p0, px, py, vx, vy on the stored windows: within 5x the float
-  oracle's distance to FP64 on the same windows (+1e-6).
-Over thousands of steps the float oracle itself drifts about 1e-5 from FP64
-(batched scenes at 2000 steps: 0.65e-5 .. 1.2e-5), so no FP32 solve can meet
-a fixed 1e-5 there; the GPU's FP32 transforms drift 2-3.6x as far (the error
-grows close to linearly in the step count on the scenes measured), which the
-5x bound admits and every test reports.
+* receiver series: <= 1e-5 against the FP64 oracle (the metric's bound), or
+  -- where the float oracle is itself more than 2e-5 from FP64, as the
+  L-shape is after 4000 steps -- within half the float oracle's own
+  distance; and <= 1e-5 against the float oracle wherever that oracle is
+  within 5e-6 of FP64;
+* final p0, px, py, vx, vy on the stored windows: no farther from FP64 than
+  the float oracle (the reference's own build) is (+1e-6).
+Over thousands of steps an FP32 solve drifts from FP64 linearly with the
+step count: every derivative scales the discrete wave speed by the round-trip
+gain of its transform, and float constants bias that gain.  The reference's
+float build drifts about 1e-5 over 2000 steps (its derivative factors are
+computed in float); the GPU divides its filters by its transforms' modelled
+gain (csrc/transform_gain.hpp) and stays at 0.3-0.9 of that distance.
 
 With PSTD_PARITY_REPORT=<path> every test appends its measured errors to that
 file as JSON lines.
@@ -37,8 +39,9 @@ from parity import FIELDS, rel
 pytestmark = pytest.mark.gpu
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-REC_TOL = 1e-5
-FLOOR_FACTOR = 5      # x the float oracle's own distance to FP64
+REC_TOL = 1e-5       # receivers vs FP64 (the metric's bound)
+REC_FLOOR_SHARE = 0.5  # where the float oracle is > 2 REC_TOL from FP64: this share of its distance
+FIELD_FACTOR = 1.0   # fields: x the float oracle's own distance to FP64
 
 
 def _fixture(name):
@@ -78,11 +81,11 @@ def _check(fx, key, receivers, snapshot, label):
     out["fields_whole_scene_f32_vs_f64"] = dict(zip(FIELDS, (float(x) for x in fx[f"{key}/floor"])))
     _report(out)
     floor = out["rec_f32_vs_f64"]
-    assert out["rec_vs_f64"] <= max(REC_TOL, FLOOR_FACTOR * floor + 1e-6), out
-    if floor <= REC_TOL / FLOOR_FACTOR:
+    assert out["rec_vs_f64"] <= max(REC_TOL, REC_FLOOR_SHARE * floor), out
+    if floor <= REC_TOL / 2:   # (where the float oracle is well inside the bound itself)
         assert out["rec_vs_f32"] <= REC_TOL, out
     for f, e in fields.items():
-        assert e["vs_f64"] <= FLOOR_FACTOR * e["f32_vs_f64"] + 1e-6, (f, e)
+        assert e["vs_f64"] <= FIELD_FACTOR * e["f32_vs_f64"] + 1e-6, (f, e)
     return out
 
 
