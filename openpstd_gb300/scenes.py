@@ -229,10 +229,11 @@ def large_square(seed: int = 0, half: int = 4096, steps: int = 1000, pml: int = 
                  receivers_near: Optional[Tuple[float, float]] = None) -> PSTDConfiguration:
     """2x2 domains of half x half cells with PML (alpha=1) on the outer edges.
 
-    ``receivers_near=(r0, r1)`` places every receiver at a seeded distance
-    between r0 and r1 metres from a seeded speaker (same speakers as without
-    it), so that a solve of a few hundred steps -- the pulse travels
-    c*dt = 0.1 m per step at CFL 0.5 -- already records the pulse."""
+    ``receivers_near=(r0, r1)`` places every receiver so that the cell it
+    samples lies at a seeded distance between r0 and r1 metres from a seeded
+    speaker (same speakers as without it), so that a solve of a few dozen
+    steps -- the pulse travels c*dt = 0.1 m per step at CFL 0.5 -- already
+    records the pulse."""
     rng = np.random.default_rng(seed)
     conf = PSTDConfiguration()
     base_settings(conf, steps, dx=dx, pml=pml)
@@ -253,13 +254,19 @@ def large_square(seed: int = 0, half: int = 4096, steps: int = 1000, pml: int = 
         for _ in range(1000):
             r = rng.uniform(*receivers_near)
             a = rng.uniform(0.0, 2.0 * math.pi)
-            gx = math.floor((sx + r * math.cos(a)) / dx)
-            gy = math.floor((sy + r * math.sin(a)) / dx)
+            # the cell the receiver samples; the reference reads p0(rel.x, rel.y)
+            # with rows = y (kernel/core/Receiver.cpp:82), so a receiver at
+            # domain offset (u, v) samples the cell at offset (v, u)
+            tx = math.floor((sx + r * math.cos(a)) / dx)
+            ty = math.floor((sy + r * math.sin(a)) / dx)
+            dom = [(x0, y0, nx, ny) for x0, y0, nx, ny in rects if x0 <= tx < x0 + nx and y0 <= ty < y0 + ny]
+            if not dom:
+                continue
+            x0, y0, nx, ny = dom[0]
+            gx, gy = x0 + (ty - y0), y0 + (tx - x0)
             p = (float(f32((gx + 0.25) * f32(dx))), float(f32((gy + 0.25) * f32(dx))), 0.0)
             qx, qy = int(f32(p[0]) / f32(dx)), int(f32(p[1]) / f32(dx))
-            # inside one domain, with the transposed lookup (row = x offset) in range
-            if (qx, qy) == (gx, gy) and any(x0 <= qx < x0 + nx and y0 <= qy < y0 + ny and qx - x0 < ny
-                                            and qy - y0 < nx for x0, y0, nx, ny in rects):
+            if (qx, qy) == (gx, gy) and x0 <= qx < x0 + nx and y0 <= qy < y0 + ny and qx - x0 < ny and qy - y0 < nx:
                 conf.Receivers.append(p)
                 break
         else:
