@@ -253,13 +253,18 @@ int pstd_work_counts(pstd_kernel* k, int64_t* cells, int64_t* air_cells, int32_t
  * pstd_server_submit builds the scene on the host and queues it; every
  * pstd_server_tick admits queued requests in arrival order while their
  * fields fit (admission by HBM footprint), advances all active scenes
- * together -- one stage-kernel launch per strip length and RK stage over the
- * strips of all of them, captured as CUDA graphs per membership -- by
- * min(max_steps, steps left of the scene closest to completion), and hands
- * finished scenes' receiver series (and, with PSTD_REQ_FINAL_FRAME, their
- * last p0 frame) to the host.  Results equal a solo pstd_create +
- * pstd_advance of the same scene with the same kernel variants.  One thread
- * drives a server; calls are not re-entrant. */
+ * together and hands finished scenes' receiver series (and, with
+ * PSTD_REQ_FINAL_FRAME, their last p0 frame) to the host.  By default every
+ * RK stage is one persistent stage-kernel launch per strip length over
+ * device-resident job tables that admissions and completions update in
+ * place (the step graphs are captured again only when a table grows or a
+ * new strip length appears); a tick runs up to max_steps steps and each
+ * scene stops on the device at its own step count.  PSTD_SERVE_FORM=merged
+ * uses one merged launch per stage; PSTD_SERVE_PERSISTENT=0 rebuilds the
+ * plan per membership change and advances all scenes to the nearest
+ * completion.  Results equal a solo pstd_create + pstd_advance of the same
+ * scene with the same kernel configurations.  One thread drives a server;
+ * calls are not re-entrant. */
 typedef struct pstd_server pstd_server;
 #define PSTD_REQ_QUEUED    0
 #define PSTD_REQ_ACTIVE    1
@@ -310,15 +315,15 @@ int pstd_server_launch_stats(pstd_server* s, int64_t* out);
  * and a message giving the bytes needed (use pstd_create for those).
  * The first call on a device takes the array's device address
  * (cudaGetSymbolAddress) with that device current and keeps it for the
- * process; make that first call before any stream capture.  A
- * cudaDeviceReset unloads the array with the module, so that address no
- * longer holds: after a reset, do not call this entry point again in the
- * same process.  Every call shares the array and clears it
+ * process.  A cudaDeviceReset unloads the array with the module, so that
+ * address no longer holds: after a reset, do not call this entry point
+ * again in the same process.  Every call shares the array and clears it
  * itself; calls whose GPU work overlaps (other streams, other threads on one
  * device) race on it.  The plan upload is a pageable host-to-device copy,
  * so the call waits for work already queued on `stream`.  Each strip length
- * runs the first plain stage-kernel variant compiled for it (no autotuning),
- * so results match pstd_create + pstd_advance to FP32 rounding. */
+ * runs the first one-CTA-per-job FP32 stage-kernel variant compiled for it
+ * (no autotuning; pstd_create with PSTD_VARIANT=0 runs the same ones), so
+ * results match pstd_create + pstd_advance to FP32 rounding. */
 #define PSTD_NOALLOC_SCRATCH_BYTES (16u << 20)
 int pstd_solve_noalloc(const pstd_config* config, int32_t n_steps, float* frame_dev, int64_t frame_len,
                        float* receivers_dev, int64_t receivers_len, void* stream);
