@@ -252,6 +252,18 @@ struct Kernel {
     size_t frame_floats = 0;
     DevBuf<int> dframe_doms;
     DevBuf<long long> dframe_off;
+    // run()'s frame slots (device) and their pinned host staging, kept across
+    // runs; made at create for frames of up to 8 slots in 128 MiB
+    PinnedBuf run_stage;
+    DevBuf<float> run_slots;
+    // frames in flight of run() for slots of `slot` floats: up to 8 within 64 MiB, at least 3
+    static int run_slot_count(size_t slot) {
+        return (int)std::min<size_t>(8, std::max<size_t>(3, (size_t(64) << 20) / (std::max<size_t>(slot, 1) * sizeof(float))));
+    }
+    void reserve_run_slots(size_t floats) {
+        run_stage.alloc(floats);
+        if (run_slots.n < floats) run_slots.alloc(floats);
+    }
 
     // staged (TMA) form: a 2-D tensor map per (domain, field, state set) and
     // the error word a CTA sets when a staged copy does not arrive in time
@@ -668,6 +680,11 @@ struct Kernel {
         }
         dframe_doms.upload(frame_doms);
         dframe_off.upload(frame_off);
+        if (scenes.size() == 1) {   // run()'s frame slots, made here so that run() only copies
+            const size_t slot = frame_floats + (size_t)std::max(n_rec, 1);
+            const size_t total = slot * run_slot_count(slot);
+            if (total * sizeof(float) <= (size_t(128) << 20)) reserve_run_slots(total);
+        }
 
         // ---- tables and the job plan (autotuned, or from the plan cache), then the launch form
         for (size_t i = 0; i < buckets.size(); i++) {

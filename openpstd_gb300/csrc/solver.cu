@@ -72,11 +72,10 @@ static int run_frames(Kernel* k, const pstd_callbacks* cb, int save_nth = 0, int
     // device runs further ahead of a host whose callbacks take uneven time.
     const size_t slot = frame_floats + (size_t)std::max(k->n_rec, 1);
     const size_t slot_bytes = (frame_floats + (size_t)k->n_rec) * sizeof(float);
-    const int K = (int)std::min<size_t>(8, std::max<size_t>(3, (size_t(64) << 20) / (slot * sizeof(float))));
-    PinnedBuf stage;
-    stage.alloc(slot * K);
-    DevBuf<float> dslots;
-    dslots.alloc(slot * K);
+    const int K = Kernel::run_slot_count(slot);
+    k->reserve_run_slots(slot * K);   // (made at create for the common frame size: nothing to do then)
+    PinnedBuf& stage = k->run_stage;
+    DevBuf<float>& dslots = k->run_slots;
     struct Sync {   // events and the copy stream, released on every exit
         std::vector<cudaEvent_t> ready, done;
         cudaStream_t copy = nullptr;
