@@ -2,16 +2,19 @@
 restated, double = FP64 build), through the C ABI.
 
 Tolerances:
-* receiver time series: relative L2 <= 1e-5 against the float oracle and
-  against the FP64 oracle wherever the float oracle is
-  itself within 1e-5/3 of FP64; receivers the wave has not reached carry
-  only round-off, and there the GPU must stay within 3x the float oracle's
-  distance to FP64;
+* receiver time series: relative L2 <= 1e-5 against the FP64 oracle wherever
+  the float oracle is itself within 1e-5 of FP64, and <= 1e-5 against the
+  float oracle where that is within 1e-5/3 of FP64; receivers the wave has
+  not reached carry only round-off, and there the GPU must stay within 3x
+  the float oracle's distance to FP64;
 * final p0/px/py/vx/vy over the whole scene: the GPU's distance to the FP64
-  oracle must stay within 3x the float oracle's own distance to FP64 (+1e-6).
+  oracle must stay within 2x the float oracle's own distance to FP64 (+1e-6).
   A fixed 1e-5 is not attainable by any FP32 build on absorbing scenes
-  (the float oracle itself is ~1e-4 from FP64 on the 500-step square), so the
+  (px - py is an undamped round-off walk in the split-field formulation; the
+  float oracle itself is ~1e-4 from FP64 on the 500-step square), so the
   bar is the reference-float noise floor measured on the same inputs.
+  (Measured: reached receivers 0.5-2e-6 from FP64, fields 0.6-1.55x the
+  float oracle's distance.)
 """
 import json
 import os
@@ -46,10 +49,13 @@ def check_parity(oracle_mod, conf, steps, rec_tol=1e-5, threads=8):
     f32_, f64_ = scene_fields(n, s32.snapshot), scene_fields(n, s64.snapshot)
     report = {"rec_vs_f32": rel(rg, r32), "rec_vs_f64": rel(rg, r64), "rec_floor": rel(r32, r64)}
     if r64.size:
-        # the strict bar holds where the float reference itself meets it;
-        # receivers the wave has not reached yet carry only round-off
-        bar = max(rec_tol, 3 * report["rec_floor"] + 1e-6)
-        assert report["rec_vs_f64"] <= bar, report
+        # rec_tol against FP64 wherever the float reference itself meets it;
+        # receivers the wave has not reached yet carry only round-off (the
+        # float reference is then far from FP64 too)
+        if report["rec_floor"] <= rec_tol:
+            assert report["rec_vs_f64"] <= rec_tol, report
+        else:
+            assert report["rec_vs_f64"] <= 3 * report["rec_floor"], report
         if report["rec_floor"] <= rec_tol / 3:
             assert report["rec_vs_f32"] <= rec_tol, report
     for f in FIELDS:
@@ -59,9 +65,9 @@ def check_parity(oracle_mod, conf, steps, rec_tol=1e-5, threads=8):
         with open(path, "a") as fh:
             fh.write(json.dumps({"case": f"{conf.Settings.framecount()}-frame scene, {steps} steps, "
                                          f"{len(conf.Domains)} domains", **report}) + "\n")
-    for f in FIELDS:
+    for f in FIELDS:   # px - py is an undamped round-off walk: within 2x the float reference's own error
         err, floor = report[f]
-        assert err <= 3 * floor + 1e-6, (f, err, floor)
+        assert err <= 2 * floor + 1e-6, (f, err, floor)
     return k, report
 
 
