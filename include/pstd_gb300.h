@@ -102,14 +102,28 @@ typedef struct pstd_config {
  *   Called when frame % SaveNth == 0, before PML attenuation (kernel/Solver.cpp:80-84).
  * write_sample: n == 1 sample of receiver `receiver` at time step start_sample
  *   (kernel/Solver.cpp:86-91).
+ * frame_buffer (optional, no reference counterpart): asked for a frame's
+ *   destination when the frame is formed, some frames before its write_frame;
+ *   returns host memory for n floats that stays untouched by the caller until
+ *   write_frame(frame, domain) hands the same pointer back, filled (the
+ *   caller then owns it: no copy).  Memory pinned or registered with
+ *   pstd_host_register is copied into directly by the device; NULL (or a
+ *   NULL callback) uses the library's own staging and write_frame's data is
+ *   valid only during the call.
  * A non-zero return stops the run at the next frame boundary with
- * PSTD_ERR_CALLBACK.  log may be NULL. */
+ * PSTD_ERR_CALLBACK.  log and frame_buffer may be NULL. */
 typedef struct pstd_callbacks {
     void* user;
     int (*write_frame)(void* user, int32_t frame, int32_t domain, const float* data, int64_t n);
     int (*write_sample)(void* user, int32_t start_sample, int32_t receiver, const float* data, int64_t n);
     void (*log)(void* user, int32_t level, const char* message);
+    float* (*frame_buffer)(void* user, int32_t frame, int32_t domain, int64_t n);
 } pstd_callbacks;
+
+/* Page-lock host memory for direct device copies (frame_buffer destinations);
+ * wraps cudaHostRegister / cudaHostUnregister.  No reference counterpart. */
+int pstd_host_register(void* ptr, int64_t bytes);
+int pstd_host_unregister(void* ptr);
 
 typedef struct pstd_kernel pstd_kernel;
 

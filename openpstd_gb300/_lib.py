@@ -32,11 +32,12 @@ WRITE_FRAME = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_int32, ct
 WRITE_SAMPLE = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
                                 ctypes.POINTER(ctypes.c_float), ctypes.c_int64)
 LOG = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int32, ctypes.c_char_p)
+FRAME_BUFFER = ctypes.CFUNCTYPE(ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int64)
 
 
 class c_callbacks(ctypes.Structure):
     _fields_ = [("user", ctypes.c_void_p), ("write_frame", WRITE_FRAME), ("write_sample", WRITE_SAMPLE),
-                ("log", LOG)]
+                ("log", LOG), ("frame_buffer", FRAME_BUFFER)]
 
 
 # every symbol the header declares, with its signature
@@ -75,6 +76,8 @@ SIGNATURES = {
     "pstd_server_cancel": (ctypes.c_int, [_vp, _i64]),
     "pstd_stage_variants": (ctypes.c_int, [_i32, ctypes.c_char_p, _i32, _P(_i32)]),
     "pstd_transform_gain": (ctypes.c_int, [_i32, _P(_i32), _i32, _i32, _i32, _P(ctypes.c_double)]),
+    "pstd_host_register": (ctypes.c_int, [_vp, _i64]),
+    "pstd_host_unregister": (ctypes.c_int, [_vp]),
     "pstd_server_stats": (ctypes.c_int, [_vp, _P(_i64)]),
     "pstd_server_launch_stats": (ctypes.c_int, [_vp, _P(_i64)]),
     "pstd_solve_noalloc": (ctypes.c_int, [_P(c_config), _i32, _vp, _i64, _vp, _i64, _vp]),

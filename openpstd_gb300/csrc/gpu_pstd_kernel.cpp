@@ -4,6 +4,7 @@
 
 #include <cmath>
 #include <cstring>
+#include <mutex>
 
 namespace pstd_gb300 {
 
@@ -145,12 +146,51 @@ struct RunCtx {
     std::exception_ptr error;
 };
 
+// Frame vectors handed to WriteFrame are recycled: a fresh multi-megabyte
+// vector is faulted in and zeroed by the OS on every allocation, which costs
+// more than the copy itself.  A frame returns to the pool when the callee
+// drops its last reference (the shared_ptr's deleter), from any thread; the
+// pool outlives every run (never destroyed, so late deleters stay valid).
+struct FramePool {
+    std::mutex m;
+    std::vector<PSTD_FRAME*> free;
+    PSTD_FRAME_PTR take(const float* data, int64_t n) {
+        PSTD_FRAME* v = nullptr;
+        {
+            std::lock_guard<std::mutex> lock(m);
+            for (size_t i = 0; i < free.size(); i++)
+                if (free[i]->capacity() >= (size_t)n) {
+                    v = free[i];
+                    free.erase(free.begin() + (long)i);
+                    break;
+                }
+        }
+        if (!v) v = new PSTD_FRAME();
+        v->assign(data, data + n);
+        return PSTD_FRAME_PTR(v, [this](PSTD_FRAME* q) { give(q); });
+    }
+    void give(PSTD_FRAME* q) {
+        {
+            std::lock_guard<std::mutex> lock(m);
+            if (free.size() < 16) {
+                free.push_back(q);
+                return;
+            }
+        }
+        delete q;
+    }
+};
+
+FramePool& frame_pool() {
+    static FramePool* pool = new FramePool();
+    return *pool;
+}
+
 int frame_bridge(void* user, int32_t frame, int32_t domain, const float* data, int64_t n) {
     auto* ctx = static_cast<RunCtx*>(user);
     try {
         // the callee may keep the frame (kernel/KernelInterface.h:285-290)
-        auto f = std::make_shared<PSTD_FRAME>(data, data + n);
-        ctx->cb->WriteFrame(frame, domain, f);
+        ctx->cb->WriteFrame(frame, domain, frame_pool().take(data, n));
         return 0;
     } catch (...) {
         ctx->error = std::current_exception();

@@ -94,7 +94,8 @@ static int run_frames(Kernel* k, const pstd_callbacks* cb, int save_nth = 0, int
     }
     CK(cudaStreamCreateWithFlags(&sy.copy, cudaStreamNonBlocking));
     auto& ev = sy.done;
-    struct Pending { int frame, slot; };
+    // per frame, the caller's destination of each domain's frame (nullptr: the staging slot)
+    struct Pending { int frame, slot; std::vector<float*> dst; };
     std::deque<Pending> q;
     int status = PSTD_OK;
     auto log = [&](int lvl, const std::string& m) { if (cb && cb->log) cb->log(cb->user, lvl, m.c_str()); };
@@ -103,8 +104,9 @@ static int run_frames(Kernel* k, const pstd_callbacks* cb, int save_nth = 0, int
         float* base = stage.p + slot * p.slot;
         for (size_t i = 0; i < k->frame_doms.size(); i++) {
             int d = k->frame_doms[i];
+            const float* data = (i < p.dst.size() && p.dst[i]) ? p.dst[i] : base + foff[i];
             if (cb && cb->write_frame && status == PSTD_OK)
-                if (cb->write_frame(cb->user, p.frame, sc.doms[d].id, base + foff[i], (int64_t)fn[i]) != 0)
+                if (cb->write_frame(cb->user, p.frame, sc.doms[d].id, data, (int64_t)fn[i]) != 0)
                     status = PSTD_ERR_CALLBACK;
         }
         for (int r = 0; r < k->n_rec; r++) {
@@ -145,12 +147,26 @@ static int run_frames(Kernel* k, const pstd_callbacks* cb, int save_nth = 0, int
                             dbase + frame_floats));
             CK(cudaEventRecord(sy.ready[s], k->stream));
             CK(cudaStreamWaitEvent(sy.copy, sy.ready[s], 0));
-            if (slot_bytes) CK(cudaMemcpyAsync(base, dbase, slot_bytes, cudaMemcpyDeviceToHost, sy.copy));
+            std::vector<float*> dst;
+            if (cb && cb->frame_buffer && cb->write_frame) {
+                // the caller's own buffers: one copy per domain, the receiver row to the staging slot
+                for (size_t i = 0; i < k->frame_doms.size(); i++) {
+                    float* p = cb->frame_buffer(cb->user, f, sc.doms[k->frame_doms[i]].id, (int64_t)fn[i]);
+                    dst.push_back(p);
+                    float* to = p ? p : base + foff[i];
+                    if (fn[i]) CK(cudaMemcpyAsync(to, dbase + foff[i], fn[i] * sizeof(float), cudaMemcpyDeviceToHost, sy.copy));
+                }
+                if (k->n_rec)
+                    CK(cudaMemcpyAsync(base + frame_floats, dbase + frame_floats, (size_t)k->n_rec * sizeof(float),
+                                       cudaMemcpyDeviceToHost, sy.copy));
+            } else if (slot_bytes) {
+                CK(cudaMemcpyAsync(base, dbase, slot_bytes, cudaMemcpyDeviceToHost, sy.copy));
+            }
             CK(cudaEventRecord(ev[s], sy.copy));
-            q.push_back({f, s});
+            q.push_back({f, s, std::move(dst)});
             inflight++;
         } else {
-            q.push_back({f, -1});   // logged once every earlier frame is delivered
+            q.push_back({f, -1, {}});   // logged once every earlier frame is delivered
         }
         while (!q.empty() && q.front().slot < 0 && status == PSTD_OK) pop_front();
         while (inflight >= K && status == PSTD_OK) {
@@ -511,6 +527,20 @@ int pstd_work_counts(pstd_kernel* h, int64_t* cells, int64_t* air, int32_t* laun
     if (cells) *cells = h->k->cells;
     if (air) *air = h->k->air_cells;
     if (launches) *launches = h->k->launches_per_step();
+    return PSTD_OK;
+}
+
+int pstd_host_register(void* ptr, int64_t bytes) {
+    if (!ptr || bytes <= 0) return fail(PSTD_ERR_INVALID, "nothing to register");
+    const cudaError_t e = cudaHostRegister(ptr, (size_t)bytes, cudaHostRegisterDefault);
+    if (e != cudaSuccess) return fail(PSTD_ERR_CUDA, std::string("cudaHostRegister: ") + cudaGetErrorString(e));
+    return PSTD_OK;
+}
+
+int pstd_host_unregister(void* ptr) {
+    if (!ptr) return fail(PSTD_ERR_INVALID, "nothing to unregister");
+    const cudaError_t e = cudaHostUnregister(ptr);
+    if (e != cudaSuccess) return fail(PSTD_ERR_CUDA, std::string("cudaHostUnregister: ") + cudaGetErrorString(e));
     return PSTD_OK;
 }
 

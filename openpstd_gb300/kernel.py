@@ -92,14 +92,69 @@ def _log_bridge(target: Optional[KernelCallbackLog]):
 _COPY_CHUNK = 1 << 18            # floats per copy task (1 MiB)
 _COPY_THREADS = 8
 _copy_pool = None
+_POOL_KEEP = 32                  # free frame buffers kept per frame size
+_free_frames = {}                # size -> list of float32 arrays no frame uses
+_registered = set()              # addresses of pool buffers page-locked for direct device copies
+_DIRECT_MIN = 2 * _COPY_CHUNK    # frames of at least this many floats go straight into pool buffers
+_DIRECT_CAP = 512 << 20          # most bytes of pool buffers reserved for one scene's frames
+
+
+def _pool_take(n: int, register: bool = False) -> np.ndarray:
+    free = _free_frames.get(n)
+    raw = free.pop() if free else np.empty(n, np.float32)
+    if register and raw.ctypes.data not in _registered:
+        if _lib.lib().pstd_host_register(ctypes.c_void_p(raw.ctypes.data), raw.nbytes) == _lib.PSTD_OK:
+            _registered.add(raw.ctypes.data)
+    return raw
+
+
+class _FrameLease:
+    """Owner of a pooled frame buffer handed to a callback.  Every numpy view
+    of the frame (and every view of those) keeps the lease alive, so the
+    buffer goes back to the pool only when the callee holds no view of it."""
+    __slots__ = ("raw", "__array_interface__", "__weakref__")
+
+    def __init__(self, raw):
+        self.raw = raw
+        self.__array_interface__ = raw.__array_interface__
+
+    def __del__(self):
+        _pool_give(self.raw)
+
+
+def _pool_give(raw):
+    free = _free_frames.setdefault(raw.size, [])
+    if len(free) < _POOL_KEEP:
+        free.append(raw)
+    elif raw.ctypes.data in _registered:
+        try:
+            _registered.discard(raw.ctypes.data)
+            _lib.lib().pstd_host_unregister(ctypes.c_void_p(raw.ctypes.data))
+        except Exception:   # interpreter shutdown
+            pass
+
+
+def _reserve_frames(sizes, sets: int):
+    """Page-locked pool buffers for `sets` frames of the given domain sizes,
+    made ahead of a run (kept for later runs of scenes with those sizes)."""
+    need = {}
+    for n in sizes:
+        if n >= _DIRECT_MIN:
+            need[n] = need.get(n, 0) + sets
+    if sum(n * 4 * c for n, c in need.items()) > _DIRECT_CAP:
+        return
+    for n, c in need.items():
+        have = [a for a in _free_frames.get(n, []) if a.ctypes.data in _registered]
+        made = [_pool_take(n, register=True) for _ in range(max(0, min(c, _POOL_KEEP) - len(have)))]
+        for a in made:
+            _pool_give(a)
 
 
 def _copy_frame(ptr, n: int) -> np.ndarray:
     """A float32 array the callee owns, copied from the library's staging
-    buffer (valid only during the callback).  Large frames are copied in
-    1 MiB chunks by a small thread pool (numpy releases the GIL while it
-    copies): one host thread moves about 50 GB/s, less than a frame stream
-    of a large scene needs."""
+    buffer (valid only during the callback).  Large frames are copied into
+    recycled buffers in 1 MiB chunks by a small thread pool (numpy releases
+    the GIL while it copies)."""
     src = np.ctypeslib.as_array(ptr, shape=(n,))
     if n < 2 * _COPY_CHUNK:
         return src.copy()
@@ -107,12 +162,12 @@ def _copy_frame(ptr, n: int) -> np.ndarray:
     if _copy_pool is None:
         from concurrent.futures import ThreadPoolExecutor
         _copy_pool = ThreadPoolExecutor(min(_COPY_THREADS, os.cpu_count() or 1), thread_name_prefix="pstd-frame")
-    dst = np.empty(n, np.float32)
+    raw = _pool_take(n)
     parts = min(_COPY_THREADS, -(-n // _COPY_CHUNK))
     step = -(-n // parts)
-    list(_copy_pool.map(lambda i: np.copyto(dst[i * step:(i + 1) * step], src[i * step:(i + 1) * step]),
+    list(_copy_pool.map(lambda i: np.copyto(raw[i * step:(i + 1) * step], src[i * step:(i + 1) * step]),
                         range(parts)))
-    return dst
+    return np.asarray(_FrameLease(raw))
 
 
 class PSTDKernel(KernelInterface):
@@ -144,6 +199,11 @@ class PSTDKernel(KernelInterface):
         _lib.check(rc)
         self._h = h
         self._keep = [logcb, cbs]
+        # page-locked frame buffers for run(): the device copies large frames
+        # straight into the arrays the callbacks receive (frames in flight + 2)
+        sizes = [self.domain_info(i)["size"] for i in range(self.domain_count())]
+        frame = [nx * ny for (nx, ny), i in zip(sizes, range(len(sizes))) if not self.domain_info(i)["is_pml"]]
+        _reserve_frames(frame, min(8, max(3, (64 << 20) // max(4 * (sum(frame) + 64), 1))) + 2)
 
     def run(self, callback: KernelCallback, save_nth: int = 0, stride: int = 1):
         """Run Framecount steps with WriteFrame / WriteSample callbacks.
@@ -153,10 +213,23 @@ class PSTDKernel(KernelInterface):
         before it is copied to the host (pstd_run_sub)."""
         h = self._need()
         errors = []
+        inflight = {}   # address -> pool buffer the device copies a frame into
+
+        def _buffer(user, frame, domain, n):
+            if n < _DIRECT_MIN:
+                return None
+            raw = _pool_take(int(n), register=True)
+            if raw.ctypes.data not in _registered:   # not page-locked: let the library stage it
+                _pool_give(raw)
+                return None
+            inflight[raw.ctypes.data] = raw
+            return raw.ctypes.data
 
         def _frame(user, frame, domain, data, n):
             try:
-                callback.WriteFrame(int(frame), int(domain), _copy_frame(data, n))
+                raw = inflight.pop(ctypes.cast(data, ctypes.c_void_p).value, None)
+                arr = np.asarray(_FrameLease(raw)) if raw is not None else _copy_frame(data, n)
+                callback.WriteFrame(int(frame), int(domain), arr)
                 return 0
             except Exception as e:   # stop the run, re-raise after it returns
                 errors.append(e)
@@ -171,11 +244,17 @@ class PSTDKernel(KernelInterface):
                 return 1
 
         fcb, scb, lcb = _lib.WRITE_FRAME(_frame), _lib.WRITE_SAMPLE(_sample), _log_bridge(callback)
-        cbs = _lib.c_callbacks(None, fcb, scb, lcb)
-        if save_nth or stride != 1:
-            rc = _lib.lib().pstd_run_sub(h, ctypes.byref(cbs), int(save_nth), int(stride))
-        else:
-            rc = _lib.lib().pstd_run(h, ctypes.byref(cbs))
+        bcb = _lib.FRAME_BUFFER(_buffer)
+        cbs = _lib.c_callbacks(None, fcb, scb, lcb, bcb)
+        try:
+            if save_nth or stride != 1:
+                rc = _lib.lib().pstd_run_sub(h, ctypes.byref(cbs), int(save_nth), int(stride))
+            else:
+                rc = _lib.lib().pstd_run(h, ctypes.byref(cbs))
+        finally:
+            for raw in inflight.values():   # frames a stopped run never delivered
+                _pool_give(raw)
+            inflight.clear()
         if errors:
             raise errors[0]
         _lib.check(rc)
