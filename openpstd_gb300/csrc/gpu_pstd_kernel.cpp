@@ -5,6 +5,8 @@
 #include <cmath>
 #include <cstring>
 #include <mutex>
+#include <set>
+#include <map>
 
 namespace pstd_gb300 {
 
@@ -141,23 +143,24 @@ void log_bridge(void* user, int32_t level, const char* msg) {
     }
 }
 
-struct RunCtx {
-    KernelCallback* cb;
-    std::exception_ptr error;
-};
-
-// Frame vectors handed to WriteFrame are recycled: a fresh multi-megabyte
-// vector is faulted in and zeroed by the OS on every allocation, which costs
-// more than the copy itself.  A frame returns to the pool when the callee
-// drops its last reference (the shared_ptr's deleter), from any thread; the
-// pool outlives every run (never destroyed, so late deleters stay valid).
+// Frame vectors handed to WriteFrame are recycled and page-locked: the
+// device copies a frame straight into the vector the callee receives
+// (pstd_callbacks.frame_buffer), and a fresh multi-megabyte vector would be
+// faulted in and zeroed by the OS every time.  A vector returns to the pool
+// when the callee drops its last reference (the shared_ptr's deleter), from
+// any thread; the pool is never destroyed, so late deleters stay valid.
 struct FramePool {
     std::mutex m;
     std::vector<PSTD_FRAME*> free;
-    PSTD_FRAME_PTR take(const float* data, int64_t n) {
+    std::set<const float*> locked;   // data() of page-locked vectors
+    static constexpr size_t KEEP = 32;
+    static constexpr int64_t DIRECT_MIN = 1 << 19;   // floats: smaller frames are copied
+
+    // a vector of n floats (contents unspecified), page-locked if `lock`
+    PSTD_FRAME* take(int64_t n, bool lock) {
         PSTD_FRAME* v = nullptr;
         {
-            std::lock_guard<std::mutex> lock(m);
+            std::lock_guard<std::mutex> g(m);
             for (size_t i = 0; i < free.size(); i++)
                 if (free[i]->capacity() >= (size_t)n) {
                     v = free[i];
@@ -166,16 +169,29 @@ struct FramePool {
                 }
         }
         if (!v) v = new PSTD_FRAME();
-        v->assign(data, data + n);
+        v->resize((size_t)n);   // within capacity: data() does not move
+        if (lock) {
+            std::lock_guard<std::mutex> g(m);
+            if (!locked.count(v->data()) && pstd_host_register(v->data(), (int64_t)(v->capacity() * sizeof(float))) == PSTD_OK)
+                locked.insert(v->data());
+        }
+        return v;
+    }
+    bool is_locked(const float* p) {
+        std::lock_guard<std::mutex> g(m);
+        return locked.count(p) != 0;
+    }
+    PSTD_FRAME_PTR share(PSTD_FRAME* v) {
         return PSTD_FRAME_PTR(v, [this](PSTD_FRAME* q) { give(q); });
     }
     void give(PSTD_FRAME* q) {
         {
-            std::lock_guard<std::mutex> lock(m);
-            if (free.size() < 16) {
+            std::lock_guard<std::mutex> g(m);
+            if (free.size() < KEEP) {
                 free.push_back(q);
                 return;
             }
+            if (locked.erase(q->data())) pstd_host_unregister(q->data());
         }
         delete q;
     }
@@ -186,11 +202,43 @@ FramePool& frame_pool() {
     return *pool;
 }
 
+struct RunCtx {
+    KernelCallback* cb;
+    std::exception_ptr error;
+    std::map<const float*, PSTD_FRAME*> inflight;   // frames the device copies into pooled vectors
+};
+
+float* frame_buffer_bridge(void* user, int32_t, int32_t, int64_t n) {
+    auto* ctx = static_cast<RunCtx*>(user);
+    if (n < FramePool::DIRECT_MIN) return nullptr;
+    try {
+        PSTD_FRAME* v = frame_pool().take(n, true);
+        if (!frame_pool().is_locked(v->data())) {   // not page-locked: the library stages it
+            frame_pool().give(v);
+            return nullptr;
+        }
+        ctx->inflight[v->data()] = v;
+        return v->data();
+    } catch (...) {
+        return nullptr;
+    }
+}
+
 int frame_bridge(void* user, int32_t frame, int32_t domain, const float* data, int64_t n) {
     auto* ctx = static_cast<RunCtx*>(user);
     try {
         // the callee may keep the frame (kernel/KernelInterface.h:285-290)
-        ctx->cb->WriteFrame(frame, domain, frame_pool().take(data, n));
+        PSTD_FRAME_PTR f;
+        auto it = ctx->inflight.find(data);
+        if (it != ctx->inflight.end()) {   // the device copied it into a pooled vector: hand that over
+            f = frame_pool().share(it->second);
+            ctx->inflight.erase(it);
+        } else {
+            PSTD_FRAME* v = frame_pool().take(n, false);
+            std::memcpy(v->data(), data, (size_t)n * sizeof(float));
+            f = frame_pool().share(v);
+        }
+        ctx->cb->WriteFrame(frame, domain, f);
         return 0;
     } catch (...) {
         ctx->error = std::current_exception();
@@ -234,15 +282,17 @@ void GpuPSTDKernel::initialize_kernel(std::shared_ptr<PSTDConfiguration> config,
 
 void GpuPSTDKernel::run(std::shared_ptr<KernelCallback> callback) {
     if (!h_) throw PSTDKernelNotConfiguredException();
-    RunCtx ctx{callback.get(), nullptr};
+    RunCtx ctx{callback.get(), nullptr, {}};
     pstd_callbacks cb{};
     cb.user = &ctx;
     if (callback) {
         cb.write_frame = &frame_bridge;
         cb.write_sample = &sample_bridge;
         cb.log = &run_log_bridge;
+        cb.frame_buffer = &frame_buffer_bridge;
     }
     int rc = pstd_run(h_, &cb);
+    for (auto& kv : ctx.inflight) frame_pool().give(kv.second);   // frames a stopped run never delivered
     if (ctx.error) std::rethrow_exception(ctx.error);
     check(rc);
 }
