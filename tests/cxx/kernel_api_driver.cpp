@@ -20,9 +20,18 @@ struct Collect : KernelCallback {
     int frames = 0;
     double frame_sum = 0;
     std::vector<std::string> info;
+    bool keep = false;                      // keep every frame (big mode)
+    std::vector<PSTD_FRAME_PTR> kept;
+    std::vector<double> sums;               // per frame, at delivery
     void WriteFrame(int frame, int domain, PSTD_FRAME_PTR data) override {
         frames++;
-        for (float v : *data) frame_sum += v;
+        double s = 0;
+        for (float v : *data) s += v;
+        frame_sum += s;
+        if (keep) {
+            kept.push_back(data);
+            sums.push_back(s);
+        }
     }
     void WriteSample(int start, int receiver, std::vector<float> data) override {
         samples[receiver].insert(samples[receiver].end(), data.begin(), data.end());
@@ -62,6 +71,30 @@ int main(int argc, char** argv) {
         return 0;
     }
     int frames = argc > 2 ? std::atoi(argv[2]) : 20;
+    if (mode == "big") {
+        // 1000 x 600 cells: frames large enough for the device to copy them
+        // straight into pooled page-locked vectors; every frame is kept and
+        // summed again after the run (a vector reused while held would differ)
+        auto conf = square(frames);
+        conf->Domains[0].Size = Vec2(200.f, 120.f);
+        conf->Speakers = {Vec3(100.05f, 60.05f, 0)};
+        conf->Receivers = {Vec3(30.05f, 20.05f, 0)};
+        GpuPSTDKernel k;
+        k.initialize_kernel(conf, std::make_shared<KernelCallbackLog>());
+        auto cb = std::make_shared<Collect>();
+        cb->keep = true;
+        k.run(cb);
+        std::printf("{\"frames\": %d, \"size\": %zu, \"sums\": [", cb->frames, cb->kept.empty() ? 0 : cb->kept[0]->size());
+        for (size_t i = 0; i < cb->sums.size(); i++) std::printf("%s%.17g", i ? ", " : "", cb->sums[i]);
+        std::printf("], \"resums\": [");
+        for (size_t i = 0; i < cb->kept.size(); i++) {
+            double r = 0;
+            for (float v : *cb->kept[i]) r += v;
+            std::printf("%s%.17g", i ? ", " : "", r);
+        }
+        std::printf("]}\n");
+        return 0;
+    }
     auto conf = square(frames);
     GpuPSTDKernel k;
     k.initialize_kernel(conf, std::make_shared<KernelCallbackLog>());

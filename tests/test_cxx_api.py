@@ -48,6 +48,38 @@ def test_cxx_api_run_matches_oracle(driver, oracle_mod):
     assert np.linalg.norm(got - want) / np.linalg.norm(want) < 1e-5
 
 
+@pytest.mark.gpu
+def test_cxx_api_large_frames_owned(driver, monkeypatch):
+    """Frames of a 1000 x 600-cell domain: the device copies them straight
+    into pooled vectors handed to WriteFrame.  Every kept frame is intact
+    after the run, and the frames equal the Python API's (same variants)."""
+    monkeypatch.setenv("PSTD_VARIANT", "0")
+    frames = 6
+    out = json.loads(subprocess.check_output([driver, "big", str(frames)]))
+    assert out["frames"] == frames and out["size"] == 1000 * 600
+    assert out["sums"] == out["resums"]
+    from openpstd_gb300 import config as C
+    from openpstd_gb300.kernel import KernelCallback, PSTDKernel
+    conf = C.PSTDConfiguration.CreateDefaultConf()
+    conf.Domains = [C.DomainConf((0, 0), (200.0, 120.0), *(C.DomainConfEdge(1.0, False) for _ in range(4)))]
+    conf.Settings.SetPMLCells(40)
+    conf.Speakers = [(100.05, 60.05, 0)]
+    conf.Receivers = [(30.05, 20.05, 0)]
+    conf.Settings.SetRenderTime(float(np.float32((frames + 0.5) * float(conf.Settings.GetTimeStep()))))
+    kept = []
+
+    class Keep(KernelCallback):
+        def WriteFrame(self, frame, domain, data):
+            kept.append(data)
+
+    k = PSTDKernel()
+    k.initialize_kernel(conf)
+    k.run(Keep())
+    k.close()
+    assert len(kept) == frames
+    assert [float(np.sum(f, dtype=np.float64)) for f in kept] == pytest.approx(out["sums"], rel=1e-12, abs=1e-12)
+
+
 def test_cxx_pstdfile(pstd_lib, tmp_path):
     """pstd_gb300::PSTDFile (the reference's PSTDFile class on the C ABI),
     used from C++ over the reference's unqlite store."""
