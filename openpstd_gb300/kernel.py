@@ -96,15 +96,26 @@ _POOL_KEEP = 32                  # free frame buffers kept per frame size
 _free_frames = {}                # size -> list of float32 arrays no frame uses
 _registered = set()              # addresses of pool buffers page-locked for direct device copies
 _DIRECT_MIN = 2 * _COPY_CHUNK    # frames of at least this many floats go straight into pool buffers
-_DIRECT_CAP = 512 << 20          # most bytes of pool buffers reserved for one scene's frames
+_DIRECT_CAP = 512 << 20          # most bytes of page-locked pool buffers
+
+
+_registered_bytes = 0
 
 
 def _pool_take(n: int, register: bool = False) -> np.ndarray:
+    """A pool buffer of n floats; `register`: page-locked if that keeps all
+    page-locked pool buffers within _DIRECT_CAP bytes."""
+    global _registered_bytes
     free = _free_frames.get(n)
+    if free and register:   # prefer a buffer that is page-locked already
+        for i in range(len(free) - 1, -1, -1):
+            if free[i].ctypes.data in _registered:
+                return free.pop(i)
     raw = free.pop() if free else np.empty(n, np.float32)
-    if register and raw.ctypes.data not in _registered:
+    if register and raw.ctypes.data not in _registered and _registered_bytes + raw.nbytes <= _DIRECT_CAP:
         if _lib.lib().pstd_host_register(ctypes.c_void_p(raw.ctypes.data), raw.nbytes) == _lib.PSTD_OK:
             _registered.add(raw.ctypes.data)
+            _registered_bytes += raw.nbytes
     return raw
 
 
@@ -123,12 +134,14 @@ class _FrameLease:
 
 
 def _pool_give(raw):
+    global _registered_bytes
     free = _free_frames.setdefault(raw.size, [])
     if len(free) < _POOL_KEEP:
         free.append(raw)
     elif raw.ctypes.data in _registered:
         try:
             _registered.discard(raw.ctypes.data)
+            _registered_bytes -= raw.nbytes
             _lib.lib().pstd_host_unregister(ctypes.c_void_p(raw.ctypes.data))
         except Exception:   # interpreter shutdown
             pass
@@ -216,14 +229,14 @@ class PSTDKernel(KernelInterface):
         inflight = {}   # address -> pool buffer the device copies a frame into
 
         def _buffer(user, frame, domain, n):
-            if n < _DIRECT_MIN:
-                return None
-            raw = _pool_take(int(n), register=True)
-            if raw.ctypes.data not in _registered:   # not page-locked: let the library stage it
-                _pool_give(raw)
-                return None
-            inflight[raw.ctypes.data] = raw
-            return raw.ctypes.data
+            # a pool buffer page-locked at initialize_kernel, else the library's staging
+            free = _free_frames.get(int(n)) if n >= _DIRECT_MIN else None
+            for i in range(len(free) - 1, -1, -1) if free else ():
+                if free[i].ctypes.data in _registered:
+                    raw = free.pop(i)
+                    inflight[raw.ctypes.data] = raw
+                    return raw.ctypes.data
+            return None
 
         def _frame(user, frame, domain, data, n):
             try:
