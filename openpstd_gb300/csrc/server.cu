@@ -455,6 +455,16 @@ struct Server {
     }
 
     // ---------------------------------------------------------------- persistent form
+    // first capacity of a table: `c` entries (PSTD_SERVE_TABLE_DIVISOR=d > 1
+    // starts the tables d times smaller, so that tests exercise their growth)
+    static size_t first_cap(size_t c) {
+        static const size_t d = [] {
+            const char* e = std::getenv("PSTD_SERVE_TABLE_DIVISOR");
+            return e && std::atoi(e) > 1 ? (size_t)std::atoi(e) : (size_t)1;
+        }();
+        return std::max<size_t>(c / d, 1);
+    }
+
     // contents of v into b on the server's stream; b is reallocated (twice
     // the size needed, at least min_cap) when v does not fit.  True when the
     // device address changed.
@@ -571,7 +581,7 @@ struct Server {
         g.a.init(0, 1);
         regs.push_back(g);
         std::vector<size_t> caps;
-        for (const Region& x : regs) caps.push_back(x.a.cap ? x.a.cap : 1024);
+        for (const Region& x : regs) caps.push_back(x.a.cap ? x.a.cap : first_cap(1024));
         relayout(caps);
         *moved = true;
         return (int)regs.size() - 1;
@@ -644,7 +654,7 @@ struct Server {
         bool moved = false;
         if (!pers) {
             K.scenes.clear(); K.dom_base.clear(); K.rec_base.clear(); K.gdom.clear(); K.buckets.clear();
-            adom.init(4096, 1);
+            adom.init(first_cap(4096), 1);
             K.ddoms.alloc(adom.cap);
             regs.clear();
             K.djobs_all.alloc(1);
@@ -653,7 +663,7 @@ struct Server {
                 regs[0].L = 1024;
                 regs[0].a.init(0, 1);
                 regs[1].a.init(0, 1);
-                relayout({1 << 15, 1 << 16});
+                relayout({first_cap(1 << 15), first_cap(1 << 16)});
                 CK(prepare_stage_all(K.merged_fam));
             }
             for (Request* q : active) q->placed = false;

@@ -256,3 +256,29 @@ def test_lengths_form_takes_any_length(monkeypatch):
             want_rec, want_frame = _solo(conf, n)
             assert rel(rec, want_rec) <= 1e-6, rel(rec, want_rec)
             assert rel(frame, want_frame) <= 1e-6, rel(frame, want_frame)
+
+
+@pytest.mark.parametrize("form", ["merged", "lengths"])
+def test_persistent_tables_grow(monkeypatch, form):
+    """Tables that start 512 times smaller grow (reallocated, contents and
+    offsets kept, graphs captured again) several times as scenes join; every
+    result still equals its solo run."""
+    from openpstd_gb300.serving import Server
+    _form_env(monkeypatch, form)
+    monkeypatch.setenv("PSTD_SERVE_TABLE_DIVISOR", "512")
+    confs = _scenes(5, seed=41)
+    steps = [30, 22, 26, 18, 24]
+    with Server(512 << 20, max_scenes=8) as srv:
+        ids = [srv.submit(confs[0], steps[0])]
+        srv.tick(6)
+        ids += [srv.submit(c, n) for c, n in zip(confs[1:], steps[1:])]
+        srv.run_until_idle(6)
+        st = srv.stats()
+        assert st["done"] == 5 and st["persistent"] and st["graph_captures"] >= 3, st
+        for conf, rid, n in zip(confs, ids, steps):
+            rec, _ = srv.result(rid)
+            want, _ = _solo(conf, n)
+            if form == "merged":
+                assert np.array_equal(rec, want)
+            else:
+                assert rel(rec, want) <= 1e-6
