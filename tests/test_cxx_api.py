@@ -72,6 +72,9 @@ def test_cxx_api_large_frames_owned(driver, monkeypatch):
         def WriteFrame(self, frame, domain, data):
             kept.append(data)
 
+        def WriteSample(self, start, receiver, data):
+            pass
+
     k = PSTDKernel()
     k.initialize_kernel(conf)
     k.run(Keep())
