@@ -458,10 +458,8 @@ struct Server {
     // first capacity of a table: `c` entries (PSTD_SERVE_TABLE_DIVISOR=d > 1
     // starts the tables d times smaller, so that tests exercise their growth)
     static size_t first_cap(size_t c) {
-        static const size_t d = [] {
-            const char* e = std::getenv("PSTD_SERVE_TABLE_DIVISOR");
-            return e && std::atoi(e) > 1 ? (size_t)std::atoi(e) : (size_t)1;
-        }();
+        const char* e = std::getenv("PSTD_SERVE_TABLE_DIVISOR");   // (read at every setup: tests set it per server)
+        const size_t d = e && std::atoi(e) > 1 ? (size_t)std::atoi(e) : (size_t)1;
         return std::max<size_t>(c / d, 1);
     }
 
