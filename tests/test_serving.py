@@ -269,9 +269,10 @@ def test_persistent_tables_grow(monkeypatch, form):
     confs = _scenes(5, seed=41)
     steps = [30, 22, 26, 18, 24]
     with Server(512 << 20, max_scenes=8) as srv:
-        ids = [srv.submit(confs[0], steps[0])]
-        srv.tick(6)
-        ids += [srv.submit(c, n) for c, n in zip(confs[1:], steps[1:])]
+        ids = []
+        for c, n in zip(confs, steps):   # one scene joins per tick: each membership change grows the tables
+            ids.append(srv.submit(c, n))
+            srv.tick(3)
         srv.run_until_idle(6)
         st = srv.stats()
         assert st["done"] == 5 and st["persistent"] and st["graph_captures"] >= 3, st
