@@ -94,6 +94,16 @@ def test_cli_run_gpu_and_device_subsampling(tmp_path, monkeypatch):
         assert np.array_equal(data, full[::2, ::2].ravel())
 
 
+@pytest.fixture(scope="module")
+def kv_standin(tmp_path_factory):
+    """A key/value store with unqlite's entry points (tests/cxx/kv_standin.cpp),
+    for machines without the reference's unqlite source."""
+    so = str(tmp_path_factory.mktemp("kv") / "libkv_standin.so")
+    subprocess.check_call(["g++", "-std=c++17", "-O1", "-shared", "-fPIC", "-o", so,
+                           os.path.join(ROOT, "tests", "cxx", "kv_standin.cpp")])
+    return so
+
+
 def _cxx_cli(*args, unq=None):
     exe = os.path.join(ROOT, "openpstd_gb300", "pstd-cli")
     env = dict(os.environ)
@@ -102,17 +112,17 @@ def _cxx_cli(*args, unq=None):
     return subprocess.run([exe, *args], capture_output=True, text=True, env=env)
 
 
-def test_cxx_cli_create_and_run_stand_in(pstd_lib, tmp_path):
+def test_cxx_cli_create_and_run_stand_in(pstd_lib, kv_standin, tmp_path):
     """The C++ command line (pstd-cli, CLI/main.cpp's create and RunCommand)
     on a .pstd scene file: `create` writes the default scene; `run -M` runs
     RunCommand's sequence with the stand-in kernel and the frames and samples
-    land in the file; `run` without -g is refused (no CPU solver)."""
+    land in the file; `run` without -g is refused (no CPU solver).  The file
+    is unqlite's where the reference's unqlite source is at hand, else the
+    test key/value store's."""
     from oracle import oracle
     from openpstd_gb300.config import PSTDConfiguration
     from openpstd_gb300.pstdfile import PSTDFile
-    unq = oracle.unqlite_lib()
-    if unq is None:
-        pytest.skip("the reference's unqlite source is not available")
+    unq = oracle.unqlite_lib() or kv_standin
     p = str(tmp_path / "scene.pstd")
     r = _cxx_cli("create", p, unq=unq)
     assert r.returncode == 0, r.stderr
@@ -131,3 +141,72 @@ def test_cxx_cli_create_and_run_stand_in(pstd_lib, tmp_path):
         assert f.GetResultsFrameCount(0) == 3 and f.GetResultsFrameCount(1) == 3
         assert np.array_equal(f.GetResultsFrame(2, 1), np.full(100 * 75, 2.0, np.float32))   # 20 m x 15 m at 0.2 m
         assert np.array_equal(f.GetReceiverData(0), [0.0, 1.0, 2.0])
+
+
+def _large_scene(frames):
+    from openpstd_gb300 import config as C
+    conf = C.PSTDConfiguration.CreateDefaultConf()
+    conf.Domains = [C.DomainConf((0, 0), (200.0, 120.0), *(C.DomainConfEdge(1.0, False) for _ in range(4)))]
+    conf.Settings.SetPMLCells(40)
+    conf.Speakers = [(100.05, 60.05, 0)]
+    conf.Receivers = [(30.05, 20.05, 0)]
+    conf.Settings.SetRenderTime(float(np.float32((frames + 0.5) * float(conf.Settings.GetTimeStep()))))
+    return conf
+
+
+def test_scene_file_on_standin_store(pstd_lib, kv_standin, tmp_path):
+    """The scene-file code over the stand-in store: scene and results round trip."""
+    from openpstd_gb300.pstdfile import PSTDFile
+    conf = _large_scene(3)
+    p = str(tmp_path / "s.pstd")
+    with PSTDFile.New(p, kv_standin) as f:
+        f.SetSceneConf(conf)
+        f.InitializeResults()
+        f.SaveNextResultsFrame(0, np.arange(5, dtype=np.float32))
+        f.SaveReceiverData(0, [1.5, 2.5])
+        f.Commit()
+    with PSTDFile.Open(p, kv_standin) as g:
+        assert len(g.GetSceneConf().Domains) == 1
+        assert g.GetResultsFrameCount(0) == 1 and np.array_equal(g.GetResultsFrame(0, 0), np.arange(5, dtype=np.float32))
+        assert np.array_equal(g.GetReceiverData(0), [1.5, 2.5])
+
+
+@pytest.mark.gpu
+def test_cxx_cli_run_gpu_on_scene_file(pstd_lib, kv_standin, tmp_path, monkeypatch):
+    """`pstd-cli run -f scene.pstd -g`: RunCommand on the GB300 solver.  The
+    frames of a 1000 x 600-cell domain (large enough for the device to copy
+    them straight into the vectors CLIOutput stores) and the receiver samples
+    land in the scene file and equal the Python API's run of the same scene
+    with the same variants.  (The file's key/value store is the test stand-in
+    with unqlite's entry points.)"""
+    from openpstd_gb300.kernel import KernelCallback, PSTDKernel
+    from openpstd_gb300.pstdfile import PSTDFile
+    monkeypatch.setenv("PSTD_VARIANT", "0")
+    frames = 4
+    conf = _large_scene(frames)
+    p = str(tmp_path / "scene.pstd")
+    with PSTDFile.New(p, kv_standin) as f:
+        f.SetSceneConf(conf)
+        f.Commit()
+    r = _cxx_cli("run", "-f", p, "-g", unq=kv_standin)
+    assert r.returncode == 0, r.stderr
+    assert "Delete old results" in r.stdout
+    got_f, got_s = [], []
+
+    class Keep(KernelCallback):
+        def WriteFrame(self, frame, domain, data):
+            got_f.append(np.array(data))
+
+        def WriteSample(self, start, receiver, data):
+            got_s.extend(data)
+
+    k = PSTDKernel()
+    k.initialize_kernel(conf)
+    k.run(Keep())
+    k.close()
+    assert len(got_f) == frames and got_f[0].size == 1000 * 600
+    with PSTDFile.Open(p, kv_standin) as f:
+        assert f.GetResultsDomainCount() == 1 and f.GetResultsFrameCount(0) == frames
+        for i in range(frames):
+            assert np.array_equal(f.GetResultsFrame(i, 0), got_f[i]), i
+        assert np.array_equal(f.GetReceiverData(0), np.asarray(got_s, np.float32))
