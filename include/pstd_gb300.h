@@ -67,10 +67,25 @@ typedef struct pstd_settings {
     float wave_length;     /* (only used by spectral interpolation)   */
     float rk_coefficients[6];
     int32_t n_rk_coefficients;     /* must be 6 */
-    int32_t spectral_interpolation;/* ignored: the reference hard-disables it (kernel/core/Receiver.cpp:48) */
+    int32_t spectral_interpolation;/* 0 / 1: nearest-neighbour receivers, as the reference, which reads its
+                                      flag but hard-disables the interpolation (kernel/core/Receiver.cpp:48);
+                                      PSTD_RECEIVERS_SPECTRAL: spectral interpolation (see below) */
     int32_t PMLCells;
     int32_t SaveNth;
 } pstd_settings;
+
+/* Spectral receivers (no reference counterpart that runs: the reference's
+ * Receiver::compute_with_si, kernel/core/Receiver.cpp:85-121, is disabled and
+ * shifts by the integer grid location, :41).  The receiver at grid location
+ * (gx, gy) = world / dx, in the cell (ix, iy) = ((int)gx, (int)gy) of its
+ * container, samples p0 at the point itself: p0 of the container and of its
+ * low and high y neighbours is shifted along x by gx - ix with the windowed
+ * strip transform of the pressure derivative (Domain::calc's bands,
+ * reflection / transmission and window, factors exp(i k (gx - ix) dx) in
+ * place of the derivative's), and the shifted column ix is shifted along y by
+ * gy - iy the same way.  Not available in the serving loop and in
+ * pstd_solve_noalloc. */
+#define PSTD_RECEIVERS_SPECTRAL 2
 
 /* DomainConfEdge (kernel/KernelInterface.h:163-175) */
 typedef struct pstd_domain_edge {
@@ -341,6 +356,21 @@ int pstd_server_launch_stats(pstd_server* s, int64_t* out);
 #define PSTD_NOALLOC_SCRATCH_BYTES (16u << 20)
 int pstd_solve_noalloc(const pstd_config* config, int32_t n_steps, float* frame_dev, int64_t frame_len,
                        float* receivers_dev, int64_t receivers_len, void* stream);
+
+/* The stencils of a scene's spectral receivers, built on the host (no device
+ * needed; no reference counterpart).  Receiver r's sample after a step is
+ *   sum over rows i in [first[r], first[r+1]) of
+ *     row_weights[i] * (  sum_j<W  weights[w + j]          p0[d1](r1, nx(d1) - W + j)
+ *                       + sum_j<nx weights[w + W + j]      p0[dom](row, j)
+ *                       + sum_j<W  weights[w + W + nx + j] p0[d2](r2, j) )
+ * with rows[8 i ..] = {dom, row, d1, d2, r1, r2, W, w} (domain indices as
+ * pstd_get_metadata lists them, -1 = no band), nx = nx(dom), p0(row, column)
+ * the domain's p0 as the next step's first stage reads it.  With all arrays
+ * NULL, sizes[0..2] receive the row, weight and receiver counts; otherwise
+ * sizes holds the capacities (rows: 8 x sizes[0] int32, row_weights:
+ * sizes[0], weights: sizes[1], first: sizes[2] + 1). */
+int pstd_spectral_plan(const pstd_config* config, int32_t* rows, float* row_weights, float* weights, int32_t* first,
+                       int64_t* sizes);
 
 /* ---- scene files (.pstd) -------------------------------------------------
  * The reference's PSTDFile (shared/PSTDFile.h:161-415, shared/PSTDFile.cpp):

@@ -66,6 +66,7 @@ public:
           band_width = 0, wave_length = 0;
     std::vector<float> rk_coefficients;
     bool spectral_interpolation = false;
+    bool spectral_receivers = false;   // PSTD_RECEIVERS_SPECTRAL (no reference counterpart; not in scene files)
     int PMLCells = 0;
     int SaveNth = 1;
 
@@ -94,6 +95,8 @@ public:
     void SetBandWidth(float v) { band_width = v; }
     bool GetSpectralInterpolation() const { return spectral_interpolation; }
     void SetSpectralInterpolation(bool v) { spectral_interpolation = v; }
+    bool GetSpectralReceivers() const { return spectral_receivers; }
+    void SetSpectralReceivers(bool v) { spectral_receivers = v; }
     float GetWaveLength() const { return wave_length; }
     void SetWaveLength(float v) { wave_length = v; }
     float GetTimeStep() const { return tfactRK * gridSpacing / c1; }

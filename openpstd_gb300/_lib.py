@@ -81,6 +81,7 @@ SIGNATURES = {
     "pstd_server_stats": (ctypes.c_int, [_vp, _P(_i64)]),
     "pstd_server_launch_stats": (ctypes.c_int, [_vp, _P(_i64)]),
     "pstd_solve_noalloc": (ctypes.c_int, [_P(c_config), _i32, _vp, _i64, _vp, _i64, _vp]),
+    "pstd_spectral_plan": (ctypes.c_int, [_P(c_config), _vp, _vp, _vp, _vp, _P(_i64)]),
     "pstd_file_open": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, _i32, _P(_vp)]),
     "pstd_file_close": (None, [_vp]),
     "pstd_file_get_scene": (ctypes.c_int, [_vp, _i32, _P(c_config)]),

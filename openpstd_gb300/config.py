@@ -34,6 +34,9 @@ PSTD_DOMAIN_SIDE_ALL = 15
 PSTD_DOMAIN_SIDE_NONE = 0
 
 
+PSTD_RECEIVERS_SPECTRAL = 2   # pstd_settings.spectral_interpolation value of spectral receivers
+
+
 class PSTDSettings:
     """kernel/KernelInterface.h:44-158."""
 
@@ -50,6 +53,10 @@ class PSTDSettings:
         self.wave_length = f32(0)
         self.rk_coefficients: List[float] = list(RK_COEFFICIENTS)
         self.spectral_interpolation = False
+        # receivers: "nearest" (the reference: its spectral flag is read but the
+        # interpolation is hard-disabled, kernel/core/Receiver.cpp:48) or
+        # "spectral" (the point itself, windowed Fourier shifts along x then y)
+        self.receiver_interpolation = "nearest"
         self.PMLCells = 0
         self.SaveNth = 1
 
@@ -78,6 +85,13 @@ class PSTDSettings:
     def SetBandWidth(self, v): self.band_width = f32(v)
     def GetSpectralInterpolation(self): return self.spectral_interpolation
     def SetSpectralInterpolation(self, v): self.spectral_interpolation = bool(v)
+    def GetReceiverInterpolation(self): return self.receiver_interpolation
+
+    def SetReceiverInterpolation(self, v):
+        if v not in ("nearest", "spectral"):
+            raise ValueError("receiver interpolation is 'nearest' or 'spectral'")
+        self.receiver_interpolation = v
+
     def GetWaveLength(self): return self.wave_length
     def SetWaveLength(self, v): self.wave_length = f32(v)
     def GetRKCoefficients(self): return list(self.rk_coefficients)
@@ -203,6 +217,8 @@ class PSTDConfiguration:
             "Settings": {**{k: float(getattr(s, k)) for k in self._SETTINGS},
                          "rk_coefficients": [float(x) for x in s.rk_coefficients],
                          "spectral_interpolation": bool(s.spectral_interpolation),
+                         **({"receiver_interpolation": s.receiver_interpolation}
+                            if s.receiver_interpolation != "nearest" else {}),
                          "PMLCells": int(s.PMLCells), "SaveNth": int(s.SaveNth)},
             "Domains": [{"TopLeft": [float(d.TopLeft[0]), float(d.TopLeft[1])],
                          "Size": [float(d.Size[0]), float(d.Size[1])],
@@ -219,6 +235,7 @@ class PSTDConfiguration:
             setattr(s, k, f32(src[k]))
         s.rk_coefficients = [float(x) for x in src["rk_coefficients"]]
         s.spectral_interpolation = bool(src.get("spectral_interpolation", False))
+        s.SetReceiverInterpolation(src.get("receiver_interpolation", "nearest"))
         s.PMLCells = int(src["PMLCells"])
         s.SaveNth = int(src["SaveNth"])
         edge = lambda e: DomainConfEdge(float(e["Absorption"]), bool(e["LR"]))
@@ -301,7 +318,8 @@ class CConfig:
         for i in range(min(6, len(rk))):
             st.rk_coefficients[i] = float(rk[i])
         st.n_rk_coefficients = len(rk)
-        st.spectral_interpolation = int(bool(s.spectral_interpolation))
+        st.spectral_interpolation = (PSTD_RECEIVERS_SPECTRAL if s.receiver_interpolation == "spectral"
+                                     else int(bool(s.spectral_interpolation)))
         st.PMLCells = int(s.PMLCells); st.SaveNth = int(s.SaveNth)
         n = len(conf.Domains)
         self._domains = (c_domain_conf * max(1, n))()

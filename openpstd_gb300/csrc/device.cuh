@@ -63,6 +63,18 @@ struct DevReceiver {
     int dom, row, col;
 };
 
+// One row of a spectral receiver's stencil: the row's p0 shifted along x to
+// the receiver's column (a weighted sum over the row and the bands of its x
+// neighbours), times the row's weight in the y shift.
+struct DevSiRow {
+    int dom, row;     // the row (y index inside dom)
+    int d1, d2;       // x neighbours supplying the bands, -1 = none
+    int r1, r2;       // the same row inside d1 / d2
+    int W;            // band width
+    int w;            // weights: W (d1 cells nx1-W..nx1-1), nx (the row), W (d2 cells 0..W-1)
+    float yw;         // weight of the row in the y shift
+};
+
 struct DevSpeaker {
     float x, y;
 };

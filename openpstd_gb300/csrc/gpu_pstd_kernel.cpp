@@ -97,7 +97,7 @@ void to_c_config(const PSTDConfiguration& conf, ConfigStorage& st) {
     c.band_width = s.band_width; c.wave_length = s.wave_length;
     c.n_rk_coefficients = (int32_t)s.rk_coefficients.size();
     for (size_t i = 0; i < s.rk_coefficients.size() && i < 6; i++) c.rk_coefficients[i] = s.rk_coefficients[i];
-    c.spectral_interpolation = s.spectral_interpolation;
+    c.spectral_interpolation = s.spectral_receivers ? PSTD_RECEIVERS_SPECTRAL : (int32_t)s.spectral_interpolation;
     c.PMLCells = s.PMLCells;
     c.SaveNth = s.SaveNth;
     st.domains.clear();
@@ -335,6 +335,7 @@ std::shared_ptr<PSTDConfiguration> from_c_config(const pstd_config& c) {
     s.band_width = x.band_width; s.wave_length = x.wave_length;
     s.rk_coefficients.assign(x.rk_coefficients, x.rk_coefficients + (x.n_rk_coefficients > 6 ? 6 : x.n_rk_coefficients));
     s.spectral_interpolation = x.spectral_interpolation != 0;
+    s.spectral_receivers = x.spectral_interpolation == PSTD_RECEIVERS_SPECTRAL;
     s.PMLCells = x.PMLCells;
     s.SaveNth = x.SaveNth;
     for (int i = 0; i < c.n_speakers; i++)

@@ -24,6 +24,7 @@
 #include "../../include/pstd_gb300.h"
 #include "launch.hpp"
 #include "scene.hpp"
+#include "spectral_receivers.hpp"
 
 namespace pstd {
 
@@ -233,6 +234,12 @@ struct Kernel {
     DevBuf<DevReceiver> drec;
     DevBuf<float> dring;
     DevBuf<int> dcounter;
+    // spectral receivers: stencil rows, their weights, first row per receiver, row values
+    bool spectral = false;
+    int n_si_rows = 0;
+    DevBuf<DevSiRow> dsi_rows;
+    DevBuf<float> dsi_w, dsi_val;
+    DevBuf<int> dsi_first;
     std::vector<Bucket> buckets;
     int ring_cap = 1;
     int n_rec = 0;
@@ -415,13 +422,6 @@ struct Kernel {
                 int W = sc.window_for(n);
                 int wo = window_of(W, (int)sc.s.patcherror);
                 for (int vel = 0; vel < 2; vel++) {
-                    // reflection / transmission of the bands (kernel/core/kernel_functions.cpp:37-64)
-                    float rs = d.rho;
-                    float r1 = r.d1 >= 0 ? sc.doms[r.d1].rho : rs;
-                    float r2 = r.d2 >= 0 ? sc.doms[r.d2].rho : rs;
-                    float zn1 = r1 / rs, izn1 = rs / r1, zn2 = r2 / rs, izn2 = rs / r2;
-                    float rlw1 = (zn1 - 1) / (zn1 + 1), tlw1 = (2 * zn1) / (zn1 + 1), tlw2 = (2 * izn1) / (izn1 + 1);
-                    float rrw1 = (zn2 - 1) / (zn2 + 1), trw1 = (2 * zn2) / (zn2 + 1), trw2 = (2 * izn2) / (izn2 + 1);
                     DevJob j;
                     std::memset(&j, 0, sizeof j);
                     j.dom = base + r.dom;
@@ -429,8 +429,8 @@ struct Kernel {
                     j.W = W;
                     j.d1 = r.d1 >= 0 ? base + r.d1 : -1;
                     j.d2 = r.d2 >= 0 ? base + r.d2 : -1;
-                    if (vel) { j.R1 = -rlw1; j.T1 = tlw1; j.R2 = -rrw1; j.T2 = trw1; }
-                    else     { j.R1 = rlw1;  j.T1 = tlw2; j.R2 = rrw1;  j.T2 = trw2; }
+                    band_coefficients(d.rho, r.d1 >= 0 ? sc.doms[r.d1].rho : d.rho, r.d2 >= 0 ? sc.doms[r.d2].rho : d.rho,
+                                      vel != 0, j.R1, j.T1, j.R2, j.T2);
                     j.dtab = filter_of(L, vel, v, sc.s.dx);
                     j.wtab = wo;
                     j.L = L;
@@ -490,6 +490,18 @@ struct Kernel {
         for (auto& sc : scenes) { rec_base.push_back(nr); nr += (int)sc.receivers.size(); }
         framecount = 0;
         for (auto& sc : scenes) framecount = std::max(framecount, sc.s.framecount());
+    }
+
+    // stencils of the spectral receivers of every scene (host tables only)
+    SpectralPlan spectral_plan() {
+        SpectralPlan plan;
+        for (size_t si = 0; si < scenes.size(); si++)
+            plan_spectral_receivers(scenes[si], dom_base[si], [&](int W) {
+                const int o = window_of(W, (int)scenes[si].s.patcherror);   // may grow the table: first
+                return win.data() + o;
+            }, plan);
+        plan.first.push_back((int)plan.rows.size());
+        return plan;
     }
 
     // Layout of every domain's fields in a state set, the fixed buffer and the
@@ -668,6 +680,18 @@ struct Kernel {
             for (auto& r : scenes[si].receivers) rec.push_back({dom_base[si] + r.dom, r.row, r.col});
         n_rec = (int)rec.size();
         drec.upload(rec);
+        spectral = scenes[0].spectral;
+        for (auto& sc : scenes)
+            if (sc.spectral != spectral)
+                throw SceneError(PSTD_ERR_UNSUPPORTED, "a batch mixes spectral and nearest-neighbour receivers");
+        if (spectral) {
+            const SpectralPlan plan = spectral_plan();
+            n_si_rows = (int)plan.rows.size();
+            dsi_rows.upload(plan.rows);
+            dsi_w.upload(plan.weights);
+            dsi_first.upload(plan.first);
+            dsi_val.alloc((size_t)std::max(n_si_rows, 1));
+        }
         ring_cap = std::max(framecount, 1);
         dring.alloc((size_t)ring_cap * std::max(n_rec, 1));
         dcounter.alloc(1);
@@ -1240,7 +1264,11 @@ struct Kernel {
                                        srv.slots, srv.n_slots, st, dev_counts ? dev_counts + 5 : nullptr));
         } else {
             CK(cudaMemsetAsync(first_step.p, 0, scenes.size() * sizeof(int), st));
-            CK(launch_receivers(drec.p, n_rec, ddoms.p, sets[B].p, dring.p, ring_cap, dcounter.p, st));
+            if (spectral)
+                CK(launch_spectral_receivers(dsi_rows.p, n_si_rows, dsi_w.p, dsi_first.p, n_rec, ddoms.p, sets[B].p,
+                                             fixed.p, p0.p, dsi_val.p, dring.p, ring_cap, dcounter.p, st));
+            else
+                CK(launch_receivers(drec.p, n_rec, ddoms.p, sets[B].p, dring.p, ring_cap, dcounter.p, st));
         }
         for (auto e : tmp) cudaEventDestroy(e);   // destruction is deferred until the event completes
     }

@@ -113,6 +113,13 @@ cudaError_t launch_speakers(const DevDomain* doms, const int* x0, const int* y0,
                             int n_spk, float dx, float bw, float* set, float* fixed, float* p0, cudaStream_t st);
 cudaError_t launch_receivers(const DevReceiver* rec, int n_rec, const DevDomain* doms, const float* set, float* ring,
                              int cap, int* counter, cudaStream_t st);
+// spectral receivers: every stencil row's x-shifted, y-weighted p0 into rowval
+// (one warp per row), then receiver r's sample = the sum of rowval over
+// rows [first[r], first[r + 1]) into the ring, and the counter + 1
+cudaError_t launch_spectral_receivers(const DevSiRow* rows, int n_rows, const float* weights, const int* first,
+                                      int n_rec, const DevDomain* doms, const float* set, const float* fixed,
+                                      const float* p0, float* rowval, float* ring, int cap, int* counter,
+                                      cudaStream_t st);
 // serving loop: one sample per receiver into its scene's ring at the scene's
 // step count, then every listed slot's step count + 1 -- only for scenes below
 // their step limit (counts: n_rec and n_slots read from device memory,

@@ -182,6 +182,69 @@ __global__ void receiver_kernel(const DevReceiver* rec, int n_rec, const DevDoma
     if (threadIdx.x == 0) *counter = step + 1;
 }
 
+// p0 of a cell after the step, as the next step's first stage reads it:
+// the stale p0 array of PML domains, else px + py (kernel/Solver.cpp:85)
+__device__ __forceinline__ float p0_after_step(const DevDomain& d, const float* set, const float* fixed,
+                                               const float* p0, long long e) {
+    if (d.pml) return p0[d.o_p0 + e];
+    const float* b = d.fixed ? fixed : set;
+    return __fadd_rn(b[d.o_px + e], b[d.o_py + e]);
+}
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Spectral receivers, part 1: one warp per stencil row.  The x shift of the
+// row to the receiver's column is a fixed linear map of the windowed strip
+// (the bands of the x neighbours blended with the row's ends, as the pressure
+// derivative gathers them), so it is a dot product with precomputed weights.
+__global__ void si_rows_kernel(const DevSiRow* __restrict__ rows, int n_rows, const float* __restrict__ wt,
+                               const DevDomain* doms, const float* __restrict__ set, const float* __restrict__ fixed,
+                               const float* __restrict__ p0, float* rowval) {
+    const int lane = threadIdx.x & 31;
+    const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (i >= n_rows) return;
+    const DevSiRow q = rows[i];
+    const DevDomain d = doms[q.dom];
+    const float* w = wt + q.w;
+    float acc = 0.f;
+    if (q.d1 >= 0) {
+        const DevDomain a = doms[q.d1];
+        const long long e = (long long)q.r1 * a.pitch_p + (a.nx - q.W);
+        for (int j = lane; j < q.W; j += 32) acc = fmaf(w[j], p0_after_step(a, set, fixed, p0, e + j), acc);
+    }
+    {
+        const long long e = (long long)q.row * d.pitch_p;
+        for (int j = lane; j < d.nx; j += 32) acc = fmaf(w[q.W + j], p0_after_step(d, set, fixed, p0, e + j), acc);
+    }
+    if (q.d2 >= 0) {
+        const DevDomain b = doms[q.d2];
+        const long long e = (long long)q.r2 * b.pitch_p;
+        for (int j = lane; j < q.W; j += 32)
+            acc = fmaf(w[q.W + d.nx + j], p0_after_step(b, set, fixed, p0, e + j), acc);
+    }
+    acc = warp_sum(acc);
+    if (lane == 0) rowval[i] = q.yw * acc;
+}
+
+// part 2: one warp per receiver sums its rows (a fixed order: deterministic)
+__global__ void si_receiver_kernel(const int* __restrict__ first, int n_rec, const float* __restrict__ rowval,
+                                   float* ring, int ring_cap, int* counter) {
+    const int step = *counter;
+    const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int r = threadIdx.x >> 5; r < n_rec; r += nw) {
+        float acc = 0.f;
+        for (int k = first[r] + lane; k < first[r + 1]; k += 32) acc += rowval[k];
+        acc = warp_sum(acc);
+        if (lane == 0) ring[(long long)(step % ring_cap) * n_rec + r] = acc;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) *counter = step + 1;
+}
+
 __global__ void server_receiver_kernel(const DevSrvReceiver* rec, int n_rec, const DevDomain* doms,
                                        const float* __restrict__ set, float* aux, int* scene_step,
                                        const int* scene_limit, const int* slots, int n_slots, const int* counts) {
@@ -251,6 +314,15 @@ cudaError_t launch_speakers(const DevDomain* doms, const int* x0, const int* y0,
 cudaError_t launch_receivers(const DevReceiver* rec, int n_rec, const DevDomain* doms, const float* set, float* ring,
                              int cap, int* counter, cudaStream_t st) {
     receiver_kernel<<<1, 256, 0, st>>>(rec, n_rec, doms, set, ring, cap, counter);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_spectral_receivers(const DevSiRow* rows, int n_rows, const float* weights, const int* first,
+                                      int n_rec, const DevDomain* doms, const float* set, const float* fixed,
+                                      const float* p0, float* rowval, float* ring, int cap, int* counter,
+                                      cudaStream_t st) {
+    if (n_rows > 0) si_rows_kernel<<<(n_rows + 7) / 8, 256, 0, st>>>(rows, n_rows, weights, doms, set, fixed, p0, rowval);
+    si_receiver_kernel<<<1, 256, 0, st>>>(first, n_rec, rowval, ring, cap, counter);
     return cudaGetLastError();
 }
 

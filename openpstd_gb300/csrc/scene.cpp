@@ -322,6 +322,7 @@ void Scene::build(const pstd_config* cfg) {
     if (!(s.dx > 0) || !(s.c1 > 0) || !(s.tfactRK > 0) || !(s.rho > 0))
         throw SceneError(PSTD_ERR_INVALID, "grid spacing, sound speed, CFL factor and density must be positive");
     if (s.save_nth <= 0) throw SceneError(PSTD_ERR_INVALID, "SaveNth must be positive");
+    spectral = st.spectral_interpolation == PSTD_RECEIVERS_SPECTRAL;
     if (s.window() <= 0) throw SceneError(PSTD_ERR_INVALID, "patch error gives an empty window");
     if (cfg->n_domains <= 0 || !cfg->domains) throw SceneError(PSTD_ERR_INVALID, "no domains");
     if (s.pml_cells <= 0) throw SceneError(PSTD_ERR_INVALID, "PMLCells must be positive");
@@ -379,10 +380,16 @@ void Scene::build(const pstd_config* cfg) {
         if (container < 0) throw SceneError(PSTD_ERR_INVALID, "receiver " + std::to_string(i) + " lies outside every domain");
         const Domain& d = doms[container];
         int rx = (int)gx - d.x0, ry = (int)gy - d.y0;
-        if (rx < 0 || ry < 0 || rx >= d.ny || ry >= d.nx)
+        if (spectral) {
+            // the interpolated point (gx, gy) lies in the cell (rx, ry) of the container, at x offset rx
+            if (rx < 0 || ry < 0 || rx >= d.nx || ry >= d.ny)
+                throw SceneError(PSTD_ERR_UNSUPPORTED,
+                                 "receiver " + std::to_string(i) + " lies on the far edge of its domain (no cell to interpolate from)");
+        } else if (rx < 0 || ry < 0 || rx >= d.ny || ry >= d.nx) {
             throw SceneError(PSTD_ERR_UNSUPPORTED,
                              "receiver " + std::to_string(i) + " falls outside p0 under the reference's lookup p0(x offset, y offset)");
-        receivers.push_back({i, container, rx, ry});
+        }
+        receivers.push_back({i, container, rx, ry, gx, gy});
     }
 
     // strip runs: the interface combination of every row (X) / column (Y)
@@ -392,62 +399,72 @@ void Scene::build(const pstd_config* cfg) {
         if (d.rigid) continue;
         for (int ax = 0; ax < 2; ax++) {
             if (!d.update[ax]) continue;
-            Axis a = (Axis)ax;
-            int n = d.len(a);
-            int W = window_for(n);
-            for (int extra = 0; extra < 2; extra++) {   // pressure (n) and velocity (n+1) strips
-                int m = n + extra + 2 * W;
-                int L = next_pow2(m);
-                int Ld = next_pow2(2 * W + n + (extra ? 0 : 1));
-                if (L != Ld)
-                    throw SceneError(PSTD_ERR_UNSUPPORTED,
-                                     "domain " + std::to_string(d.id) + ": N+2W is a power of two, so the reference's transform "
-                                     "length and derivative-factor length disagree");
-            }
-            const std::vector<int>& lows = (a == AX_X) ? d.nb[S_LEFT] : d.nb[S_BOTTOM];
-            const std::vector<int>& highs = (a == AX_X) ? d.nb[S_RIGHT] : d.nb[S_TOP];
-            int a0 = d.lo(a), a1 = d.hi(a);
-            std::vector<char> remaining(a1 - a0, 1);
-            std::vector<std::pair<int, int>> assign(a1 - a0, {INT_MIN, INT_MIN});
-            for (size_t i = 0; i <= lows.size(); i++) {
-                int d1 = i < lows.size() ? lows[i] : -1;
-                for (size_t j = 0; j <= highs.size(); j++) {
-                    int d2 = j < highs.size() ? highs[j] : -1;
-                    int lo = a0, hi = a1;
-                    if (d1 >= 0) { lo = std::max(lo, doms[d1].lo(a)); hi = std::min(hi, doms[d1].hi(a)); }
-                    if (d2 >= 0) { lo = std::max(lo, doms[d2].lo(a)); hi = std::min(hi, doms[d2].hi(a)); }
-                    int smin = INT_MAX, smax = INT_MIN;
-                    for (int v = lo; v < hi; v++) {
-                        if (!remaining[v - a0]) continue;
-                        remaining[v - a0] = 0;
-                        smin = std::min(smin, v);
-                        smax = std::max(smax, v);
-                    }
-                    if (smin > smax) continue;
-                    for (int nbi : {d1, d2}) {
-                        if (nbi < 0) continue;
-                        const Domain& q = doms[nbi];
-                        if (smin < q.lo(a) || smax + 1 > q.hi(a))
-                            throw SceneError(PSTD_ERR_UNSUPPORTED,
-                                             "domain " + std::to_string(d.id) + ": an interface span runs past neighbour " +
-                                             std::to_string(q.id) + " (the reference reads outside its arrays)");
-                        if (q.len(a) < W)
-                            throw SceneError(PSTD_ERR_UNSUPPORTED,
-                                             "neighbour " + std::to_string(q.id) + " is narrower than the window of domain " +
-                                             std::to_string(d.id));
-                    }
-                    for (int v = smin; v <= smax; v++) assign[v - a0] = {d1, d2};
-                }
-            }
-            int start = 0;
-            for (int v = 1; v <= a1 - a0; v++) {
-                if (v == a1 - a0 || assign[v] != assign[start]) {
-                    runs.push_back({(int)k, a, start, v - start, assign[start].first, assign[start].second});
-                    start = v;
-                }
-            }
+            std::vector<StripRun> r = runs_of((int)k, (Axis)ax);
+            runs.insert(runs.end(), r.begin(), r.end());
         }
     }
+}
+
+// The runs of one domain and axis: Domain::calc's loop over (low, high)
+// neighbour pairs (kernel/core/Domain.cpp:95-391), where every pair claims the
+// contiguous span [min, max] of the strips it still finds unclaimed.
+std::vector<StripRun> Scene::runs_of(int k, Axis a) const {
+    std::vector<StripRun> out;
+    const Domain& d = doms[k];
+    int n = d.len(a);
+    int W = window_for(n);
+    for (int extra = 0; extra < 2; extra++) {   // pressure (n) and velocity (n+1) strips
+        int m = n + extra + 2 * W;
+        int L = next_pow2(m);
+        int Ld = next_pow2(2 * W + n + (extra ? 0 : 1));
+        if (L != Ld)
+            throw SceneError(PSTD_ERR_UNSUPPORTED,
+                             "domain " + std::to_string(d.id) + ": N+2W is a power of two, so the reference's transform "
+                             "length and derivative-factor length disagree");
+    }
+    const std::vector<int>& lows = (a == AX_X) ? d.nb[S_LEFT] : d.nb[S_BOTTOM];
+    const std::vector<int>& highs = (a == AX_X) ? d.nb[S_RIGHT] : d.nb[S_TOP];
+    int a0 = d.lo(a), a1 = d.hi(a);
+    std::vector<char> remaining(a1 - a0, 1);
+    std::vector<std::pair<int, int>> assign(a1 - a0, {INT_MIN, INT_MIN});
+    for (size_t i = 0; i <= lows.size(); i++) {
+        int d1 = i < lows.size() ? lows[i] : -1;
+        for (size_t j = 0; j <= highs.size(); j++) {
+            int d2 = j < highs.size() ? highs[j] : -1;
+            int lo = a0, hi = a1;
+            if (d1 >= 0) { lo = std::max(lo, doms[d1].lo(a)); hi = std::min(hi, doms[d1].hi(a)); }
+            if (d2 >= 0) { lo = std::max(lo, doms[d2].lo(a)); hi = std::min(hi, doms[d2].hi(a)); }
+            int smin = INT_MAX, smax = INT_MIN;
+            for (int v = lo; v < hi; v++) {
+                if (!remaining[v - a0]) continue;
+                remaining[v - a0] = 0;
+                smin = std::min(smin, v);
+                smax = std::max(smax, v);
+            }
+            if (smin > smax) continue;
+            for (int nbi : {d1, d2}) {
+                if (nbi < 0) continue;
+                const Domain& q = doms[nbi];
+                if (smin < q.lo(a) || smax + 1 > q.hi(a))
+                    throw SceneError(PSTD_ERR_UNSUPPORTED,
+                                     "domain " + std::to_string(d.id) + ": an interface span runs past neighbour " +
+                                     std::to_string(q.id) + " (the reference reads outside its arrays)");
+                if (q.len(a) < W)
+                    throw SceneError(PSTD_ERR_UNSUPPORTED,
+                                     "neighbour " + std::to_string(q.id) + " is narrower than the window of domain " +
+                                     std::to_string(d.id));
+            }
+            for (int v = smin; v <= smax; v++) assign[v - a0] = {d1, d2};
+        }
+    }
+    int start = 0;
+    for (int v = 1; v <= a1 - a0; v++) {
+        if (v == a1 - a0 || assign[v] != assign[start]) {
+            out.push_back({k, a, start, v - start, assign[start].first, assign[start].second});
+            start = v;
+        }
+    }
+    return out;
 }
 
 }  // namespace pstd

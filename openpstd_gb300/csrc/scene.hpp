@@ -61,6 +61,8 @@ struct Receiver {
     int id;
     int dom;          // scene index of the container
     int row, col;     // element of p0 the reference reads: p0(rel.x, rel.y) -> row rel.x, column rel.y
+                      // (spectral receivers: x offset, y offset of the cell holding the point)
+    float gx, gy;     // grid location (world / dx)
 };
 
 struct Speaker { float x, y; };   // grid coordinates after the -0.5 shift
@@ -79,11 +81,25 @@ struct Scene {
     std::vector<Receiver> receivers;
     std::vector<Speaker> speakers;
     std::vector<StripRun> runs;     // for every non-rigid domain and updated axis
+    bool spectral = false;          // receivers interpolate spectrally (PSTD_RECEIVERS_SPECTRAL)
 
     void build(const pstd_config* cfg);
+    std::vector<StripRun> runs_of(int k, Axis a) const;   // runs of any domain and axis
     int window_for(int n) const;            // window after halving for a strip of n cells
     static int next_pow2(int n);
 };
+
+// Reflection / transmission of the low (1) and high (2) interface bands of a
+// strip of a domain of density rs between neighbours of density r1 and r2
+// (kernel/core/kernel_functions.cpp:37-64, float as the reference);
+// pressure strips (vel = false) or velocity strips.
+inline void band_coefficients(float rs, float r1, float r2, bool vel, float& R1, float& T1, float& R2, float& T2) {
+    float zn1 = r1 / rs, izn1 = rs / r1, zn2 = r2 / rs, izn2 = rs / r2;
+    float rlw1 = (zn1 - 1) / (zn1 + 1), tlw1 = (2 * zn1) / (zn1 + 1), tlw2 = (2 * izn1) / (izn1 + 1);
+    float rrw1 = (zn2 - 1) / (zn2 + 1), trw1 = (2 * zn2) / (zn2 + 1), trw2 = (2 * izn2) / (izn2 + 1);
+    if (vel) { R1 = -rlw1; T1 = tlw1; R2 = -rrw1; T2 = trw1; }
+    else     { R1 = rlw1;  T1 = tlw2; R2 = rrw1;  T2 = trw2; }
+}
 
 // attenuation profile (FP64 build) of length P (pressure) or P+1 (velocity)
 void pml_profile(const Settings& s, bool velocity, bool ascending, std::vector<double>& out);

@@ -275,6 +275,7 @@ struct Server {
         if (n_steps <= 0) throw SceneError(PSTD_ERR_INVALID, "n_steps must be positive");
         auto q = std::make_unique<Request>();
         q->scene.build(cfg);
+        if (q->scene.spectral) throw SceneError(PSTD_ERR_UNSUPPORTED, "spectral receivers are not served");
         q->n_steps = n_steps;
         q->flags = flags;
         layout_scene(*q, att, att_off);

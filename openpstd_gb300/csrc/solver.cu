@@ -649,6 +649,7 @@ static int solve_noalloc(const pstd_config* config, int n_steps, float* frame_de
     kh.build_scenes(config, 1);
     const Scene& sc = kh.scenes[0];
     const int nd = (int)kh.gdom.size();
+    if (sc.spectral) return fail(PSTD_ERR_UNSUPPORTED, "spectral receivers are not available in pstd_solve_noalloc");
 
     // field layout of pstd_create (device.cuh), from the same function
     const Kernel::FieldLayout lay = kh.layout_fields();
@@ -830,6 +831,33 @@ static int solve_noalloc(const pstd_config* config, int n_steps, float* frame_de
 }
 
 }  // namespace pstd
+
+extern "C" int pstd_spectral_plan(const pstd_config* config, int32_t* rows, float* row_weights, float* weights,
+                                  int32_t* first, int64_t* sizes) {
+    if (!config || !sizes) return fail(PSTD_ERR_INVALID, "config or sizes is NULL");
+    GUARD({
+        Kernel kh;
+        kh.build_scenes(config, 1);
+        if (!kh.scenes[0].spectral) throw SceneError(PSTD_ERR_INVALID, "the scene's receivers are not spectral");
+        const SpectralPlan plan = kh.spectral_plan();
+        const int64_t need[3] = {(int64_t)plan.rows.size(), (int64_t)plan.weights.size(),
+                                 (int64_t)plan.first.size() - 1};
+        if (rows || row_weights || weights || first) {
+            if (sizes[0] < need[0] || sizes[1] < need[1] || sizes[2] < need[2])
+                throw SceneError(PSTD_ERR_INVALID, "output arrays smaller than the plan");
+            for (size_t i = 0; i < plan.rows.size(); i++) {
+                const DevSiRow& q = plan.rows[i];
+                const int32_t v[8] = {q.dom, q.row, q.d1, q.d2, q.r1, q.r2, q.W, q.w};
+                if (rows) std::memcpy(rows + 8 * i, v, sizeof v);
+                if (row_weights) row_weights[i] = q.yw;
+            }
+            if (weights) std::memcpy(weights, plan.weights.data(), plan.weights.size() * sizeof(float));
+            if (first) std::memcpy(first, plan.first.data(), plan.first.size() * sizeof(int32_t));
+        }
+        for (int j = 0; j < 3; j++) sizes[j] = need[j];
+        return 0;
+    });
+}
 
 extern "C" int pstd_solve_noalloc(const pstd_config* config, int32_t n_steps, float* frame_dev, int64_t frame_len,
                                   float* receivers_dev, int64_t receivers_len, void* stream) {

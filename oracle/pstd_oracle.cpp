@@ -409,6 +409,7 @@ struct Receiver {
     int id;
     Point grid;
     Domain<T>* container;
+    float gx = 0, gy = 0;   // grid location (spectral receivers)
 };
 
 template <class T>
@@ -417,6 +418,7 @@ struct Scene {
     std::vector<std::unique_ptr<Domain<T>>> owned;
     std::vector<Domain<T>*> domain_list;
     std::vector<Receiver<T>> receivers;
+    bool spectral = false;   // settings.spectral_interpolation == PSTD_RECEIVERS_SPECTRAL
     int number_of_domains = 0;
     int framecount = 0;
     std::map<int, Discretization<T>> disc_cache;
@@ -735,10 +737,17 @@ struct Scene {
         r.id = id;
         r.grid = Point{(int)x, (int)y};
         r.container = container;
+        r.gx = x;
+        r.gy = y;
         int rx = r.grid.x - container->top_left.x, ry = r.grid.y - container->top_left.y;
-        // p0(rel.x, rel.y): row index rel.x must be < Ny, column rel.y < Nx
-        if (rx < 0 || ry < 0 || rx >= container->size.y || ry >= container->size.x)
+        if (spectral) {
+            // the point lies in cell (rx, ry) of the container (x offset rx)
+            if (rx < 0 || ry < 0 || rx >= container->size.x || ry >= container->size.y)
+                throw OracleError(PSTD_ERR_UNSUPPORTED, "spectral receiver on the far edge of its domain");
+        } else if (rx < 0 || ry < 0 || rx >= container->size.y || ry >= container->size.x) {
+            // p0(rel.x, rel.y): row index rel.x must be < Ny, column rel.y < Nx
             throw OracleError(PSTD_ERR_UNSUPPORTED, "receiver index outside p0 after the reference's transposed lookup");
+        }
         receivers.push_back(r);
     }
 
@@ -763,6 +772,7 @@ struct Scene {
         s.band_width = st.band_width; s.pml_cells = st.PMLCells; s.save_nth = st.SaveNth;
         if (st.n_rk_coefficients != 6) throw OracleError(PSTD_ERR_INVALID, "need 6 RK coefficients");
         for (int i = 0; i < 6; i++) s.rk[i] = st.rk_coefficients[i];
+        spectral = st.spectral_interpolation == PSTD_RECEIVERS_SPECTRAL;
         if (s.dx <= 0 || s.c1 <= 0 || s.tfactRK <= 0) throw OracleError(PSTD_ERR_INVALID, "bad settings");
         // kernel/PSTDKernel.cpp:73-98,170-190
         std::vector<Domain<T>*> domains;
@@ -793,11 +803,16 @@ struct Scene {
 
     // ------------------------------------------------------------ calc
     // kernel/core/Domain.cpp:95-391
-    void calc(Domain<T>* self, CalcDirection cd, CalcType ct) {
+    // shift != nullptr: the pressure strips are shifted by *shift cells
+    // (factors exp(i k shift dx) in place of the derivative factors) into
+    // *dest -- the spectral receivers' passes
+    void calc(Domain<T>* self, CalcDirection cd, CalcType ct, const double* shift = nullptr,
+              Field2<T>* dest = nullptr) {
         std::vector<int> own_range = self->get_range(cd);
         std::vector<Domain<T>*> domains1 = (cd == CX) ? self->left : self->bottom;
         std::vector<Domain<T>*> domains2 = (cd == CX) ? self->right : self->top;
-        Field2<T>& source = (ct == PRESSURE) ? (cd == CX ? self->Lpx : self->Lpy) : (cd == CX ? self->Lvx : self->Lvy);
+        Field2<T>& source = dest ? *dest
+                          : (ct == PRESSURE) ? (cd == CX ? self->Lpx : self->Lpy) : (cd == CX ? self->Lvx : self->Lvy);
         for (size_t i = 0; i != domains1.size() + 1; i++) {
             Domain<T>* d1 = (i != domains1.size()) ? domains1[i] : nullptr;
             for (size_t j = 0; j != domains2.size() + 1; j++) {
@@ -832,7 +847,18 @@ struct Scene {
                 if (!d1) { d1 = self; side1_zero = true; }
                 if (!d2) { d2 = self; side2_zero = true; }
                 const Discretization<T>& disc = get_discretization(N_total);
-                const auto& derfact = (ct == PRESSURE) ? disc.pressure_deriv_factors : disc.velocity_deriv_factors;
+                std::vector<std::complex<T>> shift_factors;
+                if (shift) {
+                    // exp(i k shift dx) with k dx = 2 pi j / L for the bins j <= L/2 the transform uses
+                    const int Ls = (int)disc.pressure_deriv_factors.size();
+                    shift_factors.resize(Ls);
+                    for (int j = 0; j <= Ls / 2; j++) {
+                        const double a = 2.0 * M_PI * j * *shift / Ls;
+                        shift_factors[j] = std::complex<T>((T)std::cos(a), (T)std::sin(a));
+                    }
+                }
+                const auto& derfact = shift ? shift_factors
+                                    : (ct == PRESSURE) ? disc.pressure_deriv_factors : disc.velocity_deriv_factors;
                 RhoArray<T> rho = get_rho_array<T>(d1->rho, self->rho, d2->rho);
                 auto field_of = [&](Domain<T>* d) -> Field2<T>& {
                     if (ct == PRESSURE) return d->p0;
@@ -942,8 +968,43 @@ struct Scene {
         }
         for (auto& r : receivers) {
             int rx = r.grid.x - r.container->top_left.x, ry = r.grid.y - r.container->top_left.y;
-            rec_out.push_back((double)r.container->p0(rx, ry));
+            rec_out.push_back(spectral ? (double)spectral_sample(r) : (double)r.container->p0(rx, ry));
         }
+    }
+
+    // Spectral receiver (own definition; the reference's compute_with_si,
+    // kernel/core/Receiver.cpp:85-121, is disabled at :48 and shifts by the
+    // integer grid location, :41): p0 of the container D and of its low and
+    // high y neighbours shifted along x by gx - ix (calc with shift factors,
+    // as calc_domain_fields, :117-121), then D's y strips of that shifted
+    // field shifted along y by gy - iy; the value at cell (ix, iy).
+    T spectral_sample(const Receiver<T>& r) {
+        Domain<T>* D = r.container;
+        const double fx = (double)r.gx - r.grid.x, fy = (double)r.gy - r.grid.y;
+        std::vector<Domain<T>*> near{D};
+        for (auto* e : D->bottom) near.push_back(e);
+        for (auto* e : D->top) near.push_back(e);
+        std::vector<Field2<T>> shifted;
+        for (auto* e : near) {
+            Field2<T> f, g;
+            f.zeros(e->size.y, e->size.x + 1);
+            calc(e, CX, PRESSURE, &fx, &f);
+            g.zeros(e->size.y, e->size.x);
+            for (int i = 0; i < e->size.y; i++)
+                for (int j = 0; j < e->size.x; j++) g(i, j) = f(i, j);
+            shifted.push_back(std::move(g));
+        }
+        for (size_t i = 0; i < near.size(); i++) std::swap(near[i]->p0, shifted[i]);
+        Field2<T> out;
+        out.zeros(D->size.y + 1, D->size.x);
+        try {
+            calc(D, CY, PRESSURE, &fy, &out);
+        } catch (...) {
+            for (size_t i = 0; i < near.size(); i++) std::swap(near[i]->p0, shifted[i]);
+            throw;
+        }
+        for (size_t i = 0; i < near.size(); i++) std::swap(near[i]->p0, shifted[i]);
+        return out(r.grid.y - D->top_left.y, r.grid.x - D->top_left.x);
     }
 };
 
