@@ -133,10 +133,12 @@ def test_gpu_matches_oracle(oracle_mod, case):
 
 
 @pytest.mark.gpu
-def test_gpu_batch_equals_alone():
-    """Spectral receivers of a batch equal the scenes run alone, bit for bit."""
+def test_gpu_batch_equals_alone(monkeypatch):
+    """Spectral receivers of a batch equal the scenes run alone, bit for bit
+    (both on the same stage-kernel variants)."""
     from openpstd_gb300 import kernel, scenes
     from openpstd_gb300.batch import BatchKernel
+    monkeypatch.setenv("PSTD_VARIANT", "0")
     confs = [_spectral(scenes.plain_square(4, n=120, steps=30, pml=40), [(70.3, 95.6), (60.9, 60.1)]),
              _spectral(scenes.l_shape(3, scale=0.2, steps=30), _l_shape_points()[:3])]
     b = BatchKernel(confs)
