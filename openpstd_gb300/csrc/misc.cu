@@ -191,7 +191,8 @@ __device__ __forceinline__ float p0_after_step(const DevDomain& d, const float* 
     return __fadd_rn(b[d.o_px + e], b[d.o_py + e]);
 }
 
-__device__ __forceinline__ float warp_sum(float v) {
+template <class T>
+__device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
@@ -230,16 +231,17 @@ __global__ void si_rows_kernel(const DevSiRow* __restrict__ rows, int n_rows, co
     if (lane == 0) rowval[i] = q.yw * acc;
 }
 
-// part 2: one warp per receiver sums its rows (a fixed order: deterministic)
+// part 2: one warp per receiver sums its rows in FP64 (a fixed order:
+// deterministic), rounded once to the float sample
 __global__ void si_receiver_kernel(const int* __restrict__ first, int n_rec, const float* __restrict__ rowval,
                                    float* ring, int ring_cap, int* counter) {
     const int step = *counter;
     const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     for (int r = threadIdx.x >> 5; r < n_rec; r += nw) {
-        float acc = 0.f;
-        for (int k = first[r] + lane; k < first[r + 1]; k += 32) acc += rowval[k];
+        double acc = 0.0;
+        for (int k = first[r] + lane; k < first[r + 1]; k += 32) acc += (double)rowval[k];
         acc = warp_sum(acc);
-        if (lane == 0) ring[(long long)(step % ring_cap) * n_rec + r] = acc;
+        if (lane == 0) ring[(long long)(step % ring_cap) * n_rec + r] = (float)acc;
     }
     __syncthreads();
     if (threadIdx.x == 0) *counter = step + 1;
