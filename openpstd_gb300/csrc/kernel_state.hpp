@@ -326,9 +326,11 @@ struct Kernel {
     // The derivative filter of a variant: the reference's factors, 1/L, and the
     // division by the round-trip gain of the variant's transform per bin
     // (transform_gain.hpp; the tensor-core study forms are left as they are).
+    // Direct-convolution forms (v->direct = Q) take the real kernel h of the
+    // same factors instead, extended to 2L + Q floats: hx[e] = h[(e - L) mod L].
     int filter_of(int L, bool vel, const StageVariant* v, float dxf) {
         const bool study = v->bf16 || v->tc5;
-        const int form = study ? 3 : (v->shf ? 2 : 0) + (v->ctw ? 1 : 0) * 4;
+        const int form = v->direct ? 8 + v->direct : study ? 3 : (v->shf ? 2 : 0) + (v->ctw ? 1 : 0) * 4;
         auto key = std::make_tuple(L, (int)vel, v->r[0], v->r[1], v->r[2], v->r[3], dxf, form);
         auto it = filt_off.find(key);
         if (it != filt_off.end()) return it->second;
@@ -347,6 +349,24 @@ struct Kernel {
         full[0] = std::complex<double>(full[0].real(), 0);
         full[L / 2] = std::complex<double>(full[L / 2].real(), 0);   // c2r ignores the Nyquist imaginary part
         for (int j = 1; j < L / 2; j++) full[L - j] = std::conj(full[j]);
+        if (v->direct) {
+            // h[d] = (1/L) sum_k D[k] exp(2 pi i k d / L) (real: D is Hermitian)
+            std::vector<double> h(L);
+            for (int d = 0; d < L; d++) {
+                double acc = 0;
+                for (int k = 0; k < L; k++) {
+                    const double a = 2.0 * M_PI * (double)(((long long)k * d) % L) / L;
+                    acc += full[k].real() * std::cos(a) - full[k].imag() * std::sin(a);
+                }
+                h[d] = acc / L;
+            }
+            const int ne = 2 * L + v->direct;
+            std::vector<float> hx(ne + (ne & 1), 0.f);
+            for (int e = 0; e < ne; e++) hx[e] = (float)h[((e - L) % L + L) % L];
+            for (size_t e = 0; e < hx.size(); e += 2) filt.push_back(make_float2(hx[e], hx[e + 1]));
+            filt_off[key] = o;
+            return o;
+        }
         std::vector<int> pos = bin_positions(L, v->r, v->np);
         std::vector<float2> perm(L);
         for (int j = 0; j < L; j++) {

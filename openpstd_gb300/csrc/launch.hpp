@@ -62,6 +62,7 @@ struct StageVariant {
     bool tma = false;                                           // staged form: needs tensor maps and a row cap
     int ctw = 0;                                                // twiddle tables hold powers (Cfg::CTW)
     bool tc5 = false;                                           // tcgen05 TF32x3 DFT (precision study, opt-in)
+    int direct = 0;                                             // direct convolution, Q outputs per task (filter: h)
     cudaError_t (*launch)(int n_jobs, const StageArgs& a, cudaStream_t st);
     cudaError_t (*prepare)();
     size_t (*smem_for)(int row_cap);                            // dynamic shared memory of one CTA

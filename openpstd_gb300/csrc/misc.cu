@@ -18,6 +18,8 @@ const StageVariant* stage_variants_fused_m(int L, int* n);
 const StageVariant* stage_variants_fused_l(int L, int* n);
 const StageVariant* stage_variants_fused_h(int L, int* n);
 
+const StageVariant* stage_variants_direct(int L, int* n);
+
 const StageVariant* stage_variants_tma_a(int L, int* n);
 const StageVariant* stage_variants_tma_b(int L, int* n);
 
@@ -35,7 +37,8 @@ static const StageVariant* stage_variants_fused(int L, int* n) {
 
 // Per length: the fused-form variants first (the default when nothing is
 // tuned), then the TMA-staged persistent forms, then the split gather /
-// transform / epilogue forms, then the precision-study variants.  Built once, before any launch.
+// transform / epilogue forms, then the precision-study variants, then the
+// direct-convolution forms of short strips.  Built once, before any launch.
 int stage_variants(int L, const StageVariant** out) {
     static const std::vector<std::vector<StageVariant>> lists = [] {
         std::vector<std::vector<StageVariant>> all(14);
@@ -52,6 +55,9 @@ int stage_variants(int L, const StageVariant** out) {
             for (int i = 0; i < nf; i++) all[lg].push_back(f[i]);
             for (int i = 0; i < nt; i++) all[lg].push_back(tv[i]);
             for (int i = 0; i < n; i++) all[lg].push_back(v[i]);
+            int nd = 0;
+            const StageVariant* dv = stage_variants_direct(len, &nd);
+            for (int i = 0; i < nd; i++) all[lg].push_back(dv[i]);
         }
         return all;
     }();
