@@ -17,7 +17,7 @@ cell of a non-rigid domain advanced one step.
 * ``receiver_err``: the same scene solved for all 4000 steps on the GPU and
   compared with the committed oracle fixture (float = the reference's CPU
   path restated, and FP64), relative L2 of the 16 receiver series.
-* ``e2e``: the same metric through the reference-facing API: a 400-step
+* ``e2e``: the same metric through the reference-facing API: a 1000-step
   scene through ``PSTDKernel.run`` with every frame of p0 and every receiver
   sample delivered to host callbacks (SaveNth = 1), host<->device copies in
   the timed region; ``initialize_kernel`` (scene build, upload, plan) is timed
@@ -615,6 +615,20 @@ def run_ours(args):
         def WriteSample(self, start, receiver, data):
             sizes["sample_bytes"] += 4 * len(data)
 
+    # untimed warm-up of the same path (first frame buffers, callback bridge)
+    cw = conf.copy()
+    cw.Settings.SetRenderTime(float(np.float32(10.5 * float(dt))))
+    kw = kernel.PSTDKernel()
+    kw.initialize_kernel(cw)
+    class Drop(kernel.KernelCallback):
+        def WriteFrame(self, frame, domain, data):
+            pass
+
+        def WriteSample(self, start, receiver, data):
+            pass
+
+    kw.run(Drop())
+    kw.close()
     barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -671,7 +685,7 @@ def main():
     ap.add_argument("--batch-scenes", type=int, default=256)
     ap.add_argument("--plain-steps", type=int, default=20)
     ap.add_argument("--batch-steps", type=int, default=200, help="timed steps of the batched leg")
-    ap.add_argument("--e2e-steps", type=int, default=400, help="steps of the end-to-end leg")
+    ap.add_argument("--e2e-steps", type=int, default=1000, help="steps of the end-to-end leg")
     ap.add_argument("--no-batch", action="store_true", help="leave the batched leg out of the default line")
     ap.add_argument("--no-parity", action="store_true", help="leave the 4000-step receiver check out")
     ap.add_argument("--rate", type=float, default=50.0, help="serve: mean request arrivals per second")
