@@ -18,7 +18,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpstd_gb300.so")
 CLI = os.path.join(HERE, "pstd-cli")
 
-SOURCES = ["scene.cpp", "stage_fused_s.cu", "stage_fused_m.cu", "stage_fused_l.cu", "stage_fused_h.cu", "stage_tma_a.cu", "stage_tma_b.cu", "stage_small.cu", "stage_mid.cu", "stage_large.cu", "stage_huge.cu", "stage_direct.cu", "stage_all.cu", "stage_serve.cu", "misc.cu", "solver.cu", "server.cu",
+SOURCES = ["scene.cpp", "stage_fused_s.cu", "stage_fused_m.cu", "stage_fused_l.cu", "stage_fused_h.cu", "stage_tma_a.cu", "stage_tma_b.cu", "stage_small.cu", "stage_mid.cu", "stage_large.cu", "stage_huge.cu", "stage_direct.cu", "stage_toeplitz.cu", "stage_all.cu", "stage_serve.cu", "misc.cu", "solver.cu", "server.cu",
            "gpu_pstd_kernel.cpp", "pstdfile.cpp"]
 HEADERS = ["scene.hpp", "device.cuh", "launch.hpp", "stage_kernel.cuh", "stage_fused.cuh", "stage_tma.cuh", "stage_tc5.cuh",
            "transform_gain.hpp", "spectral_receivers.hpp", "kernel_state.hpp"]

@@ -858,14 +858,17 @@ struct Kernel {
         dmaps.upload(maps);
     }
 
-    // a staged copy that did not arrive in time is reported once, here
+    // a device error word (a bounded wait that gave up, a job outside a form's
+    // tile) is reported once, here
     void check_stage_error() {
         if (!derr.p) return;
         int e = 0;
         CK(cudaMemcpy(&e, derr.p, sizeof e, cudaMemcpyDeviceToHost));
         if (e) {
             CK(cudaMemset(derr.p, 0, sizeof(int)));
-            throw CudaError("a staged (TMA) copy of the stage kernel did not complete in time");
+            throw CudaError(e == 3 ? "a stage-kernel job lies outside its form's fixed tile (error 3)"
+                                   : "a bounded wait of the stage kernel (TMA copy or tensor-core commit) gave up "
+                                     "(error " + std::to_string(e) + ")");
         }
     }
 

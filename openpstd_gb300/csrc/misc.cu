@@ -19,6 +19,7 @@ const StageVariant* stage_variants_fused_l(int L, int* n);
 const StageVariant* stage_variants_fused_h(int L, int* n);
 
 const StageVariant* stage_variants_direct(int L, int* n);
+const StageVariant* stage_variants_toeplitz(int L, int* n);
 
 const StageVariant* stage_variants_tma_a(int L, int* n);
 const StageVariant* stage_variants_tma_b(int L, int* n);
@@ -38,7 +39,7 @@ static const StageVariant* stage_variants_fused(int L, int* n) {
 // Per length: the fused-form variants first (the default when nothing is
 // tuned), then the TMA-staged persistent forms, then the split gather /
 // transform / epilogue forms, then the precision-study variants, then the
-// direct-convolution forms of short strips.  Built once, before any launch.
+// direct-convolution forms of short strips (CUDA cores, then tcgen05).  Built once, before any launch.
 int stage_variants(int L, const StageVariant** out) {
     static const std::vector<std::vector<StageVariant>> lists = [] {
         std::vector<std::vector<StageVariant>> all(14);
@@ -58,6 +59,8 @@ int stage_variants(int L, const StageVariant** out) {
             int nd = 0;
             const StageVariant* dv = stage_variants_direct(len, &nd);
             for (int i = 0; i < nd; i++) all[lg].push_back(dv[i]);
+            const StageVariant* ev = stage_variants_toeplitz(len, &nd);
+            for (int i = 0; i < nd; i++) all[lg].push_back(ev[i]);
         }
         return all;
     }();

@@ -103,7 +103,7 @@ __device__ __forceinline__ float dft16_real(int k, int n, bool inv) {
     return inv ? -v : v;
 }
 
-__device__ void tc5_build_b(uint32_t* b, int tid, int nth) {
+__device__ inline void tc5_build_b(uint32_t* b, int tid, int nth) {
     for (int i = tid; i < 4 * TC5_B_WORDS; i += nth) {
         const int t = i / TC5_B_WORDS, e = i - t * TC5_B_WORDS;
         const int n = e / 32, k = e % 32;
