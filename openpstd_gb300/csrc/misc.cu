@@ -20,6 +20,7 @@ const StageVariant* stage_variants_fused_h(int L, int* n);
 
 const StageVariant* stage_variants_direct(int L, int* n);
 const StageVariant* stage_variants_toeplitz(int L, int* n);
+const StageVariant* stage_variants_toeplitz_ws(int L, int* n);
 
 const StageVariant* stage_variants_tma_a(int L, int* n);
 const StageVariant* stage_variants_tma_b(int L, int* n);
@@ -61,6 +62,8 @@ int stage_variants(int L, const StageVariant** out) {
             for (int i = 0; i < nd; i++) all[lg].push_back(dv[i]);
             const StageVariant* ev = stage_variants_toeplitz(len, &nd);
             for (int i = 0; i < nd; i++) all[lg].push_back(ev[i]);
+            const StageVariant* wv = stage_variants_toeplitz_ws(len, &nd);
+            for (int i = 0; i < nd; i++) all[lg].push_back(wv[i]);
         }
         return all;
     }();
