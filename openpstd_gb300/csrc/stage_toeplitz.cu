@@ -262,100 +262,6 @@ __device__ __forceinline__ bool toe_fits(const DevJob& job, const DevDomain& dom
     return job.W == toe::W && 2 * job.W + n <= toe::K && nout <= toe::N && job.count <= toe::ROWS;
 }
 
-// A job's 128 strips x 128 positions into the strip buffer (re / im = even /
-// odd strip, pitch Cfg::SP), the values of the plain form's gather: the
-// strip (p0 = px + py or one field), the interface bands blended with the
-// strip's mirrored ends, zero past the bands and for strips past the job.
-// Every thread takes 64 positions in 8 rounds of 8 whose loads (up to four a
-// position: band and mirror, each px + py) are all issued before any is
-// used.  Rows: a warp on 32 consecutive positions of one strip; columns: a
-// warp on 32 consecutive strips at one position (both coalesced).
-template <class C, int NTH>
-__device__ __forceinline__ void toe_gather(float2* buf, const StageArgs& A, const DevJob& job, const DevDomain& dom,
-                                           bool first, int tid) {
-    constexpr int SP = C::SP, ROWS = toe::ROWS, K = toe::K, PER = ROWS * K / NTH, B = 4;
-    static_assert(PER % B == 0, "whole rounds");
-    float* smf = reinterpret_cast<float*>(buf);
-    const bool vel = job.kind & JK_VEL, ydir = job.kind & JK_Y;
-    const int W = job.W, n = (ydir ? dom.ny : dom.nx) + (vel ? 1 : 0), count = job.count;
-    const Src S = strip_source(A, dom, vel, ydir, first);
-    Src S1{nullptr, nullptr, 0}, S3{nullptr, nullptr, 0};
-    int n1 = 0;
-    if (job.d1 >= 0) {
-        const DevDomain D1 = A.doms[job.d1];
-        S1 = strip_source(A, D1, vel, ydir, first);
-        n1 = (ydir ? D1.ny : D1.nx) + (vel ? 1 : 0);
-    }
-    if (job.d2 >= 0) S3 = strip_source(A, A.doms[job.d2], vel, ydir, first);
-    const float* wl = A.win + job.wtab;
-    const float* wr = A.win + job.wtab + W + 1;
-    for (int r0 = 0; r0 < PER; r0 += B) {
-        const float* pa[B];
-        const float* pb[B];
-        const float* ma[B];
-        const float* mb[B];
-        float wgt[B], tc[B], rc[B];
-        int kind[B];   // 0 zero, 1 strip value, 2 band
-#pragma unroll
-        for (int q = 0; q < B; q++) {
-            const int e = tid + (r0 + q) * NTH;
-            const int s = ydir ? (e & (ROWS - 1)) : (e >> 7), p = ydir ? (e >> 7) : (e & (K - 1));
-            pa[q] = pb[q] = ma[q] = mb[q] = nullptr;
-            wgt[q] = tc[q] = rc[q] = 0.f;
-            kind[q] = 0;
-            if (s >= count) continue;
-            // element `pos` of strip `strip` of source X (rows: along the strip; columns: across)
-            auto at = [&](const Src& X, int strip, int pos, const float*& a, const float*& b) {
-                const long long el = ydir ? (long long)pos * X.pitch + strip : (long long)strip * X.pitch + pos;
-                a = X.a + el;
-                b = X.b ? X.b + el : nullptr;
-            };
-            if (p < W) {
-                if (job.d1 >= 0) {
-                    const int e1 = vel ? n1 - W - 1 + p : n1 - W + p, m = vel ? W - p : W - 1 - p;
-                    at(S1, job.o1 + s, e1, pa[q], pb[q]);
-                    at(S, job.first + s, m, ma[q], mb[q]);
-                    wgt[q] = wl[p];
-                    tc[q] = job.T1;
-                    rc[q] = job.R1;
-                    kind[q] = 2;
-                }
-            } else if (p < W + n) {
-                at(S, job.first + s, p - W, pa[q], pb[q]);
-                kind[q] = 1;
-            } else if (p < 2 * W + n) {
-                const int jj = p - W - n;
-                if (job.d2 >= 0) {
-                    const int e2 = vel ? 1 + jj : jj, m = vel ? n - 2 - jj : n - 1 - jj;
-                    at(S3, job.o2 + s, e2, pa[q], pb[q]);
-                    at(S, job.first + s, m, ma[q], mb[q]);
-                    wgt[q] = wr[jj];
-                    tc[q] = job.T2;
-                    rc[q] = job.R2;
-                    kind[q] = 2;
-                }
-            }
-        }
-        float va[B], vb[B], xa[B], xb[B];
-#pragma unroll
-        for (int q = 0; q < B; q++) {
-            va[q] = pa[q] ? ldf(pa[q]) : 0.f;
-            vb[q] = pb[q] ? ldf(pb[q]) : 0.f;
-            xa[q] = ma[q] ? ldf(ma[q]) : 0.f;
-            xb[q] = mb[q] ? ldf(mb[q]) : 0.f;
-        }
-#pragma unroll
-        for (int q = 0; q < B; q++) {
-            const int e = tid + (r0 + q) * NTH;
-            const int s = ydir ? (e & (ROWS - 1)) : (e >> 7), p = ydir ? (e >> 7) : (e & (K - 1));
-            const float raw = pb[q] ? __fadd_rn(va[q], vb[q]) : va[q];
-            const float mir = mb[q] ? __fadd_rn(xa[q], xb[q]) : xa[q];
-            const float v = kind[q] == 2 ? band_value(raw, mir, tc[q], rc[q], wgt[q]) : (kind[q] == 1 ? raw : 0.f);
-            smf[2 * ((s >> 1) * SP + p) + (s & 1)] = v;
-        }
-    }
-}
-
 template <class C>
 constexpr size_t toews_smem() {
     return (size_t)C::BUF * 8 + 128 + (size_t)(2 * toe::A_WORDS + 2 * toe::E_WORDS) * 4 +
@@ -421,7 +327,7 @@ __global__ void __launch_bounds__(toews::NT, 1) stage_toe_ws(StageArgs A, int n_
                 continue;
             }
             const bool first = A.first_step[dom.scene] != 0;
-            toe_gather<C, NPROD>(buf, A, job, dom, first, ptid);
+            gather<C, NPROD, true>(buf, A, job, dom, first, ptid);
             if (ptid == 0 && g > 0 && !mbar_wait(a_free, (g - 1) & 1)) *pfail = 1;   // job g-1's operands read
             bar_sync(BAR_PROD, NPROD);
             if (*pfail) break;
@@ -531,55 +437,34 @@ __global__ void __launch_bounds__(toews::NT, 1) stage_toe_ws(StageArgs A, int n_
                 // columns: consecutive lanes on consecutive columns
                 if (s < job.count) {
 #pragma unroll
-                    for (int c0 = 0; c0 < toe::N; c0 += 16) {   // 16 stage-start loads in flight
-                        float pv[16];
-#pragma unroll
-                        for (int q = 0; q < 16; q++)
-                            pv[q] = c0 + q < nout ? prev[fo + (long long)(c0 + q) * fp + job.first + s] : 0.f;
-#pragma unroll
-                        for (int q = 0; q < 16; q++) {
-                            const int i = c0 + q;
-                            if (i < nout) {
-                                float v = rk_update(pv[q], d[i], vel, cdt, rho, c2, rinv);
-                                if (att) v = __fmul_rn(v, A.att[ao + i]);
-                                out[fo + (long long)i * fp + job.first + s] = v;
-                            }
+                    for (int i = 0; i < toe::N; i++) {
+                        if (i < nout) {
+                            const long long e = fo + (long long)i * fp + job.first + s;
+                            float v = rk_update(prev[e], d[i], vel, cdt, rho, c2, rinv);
+                            if (att) v = __fmul_rn(v, A.att[ao + i]);
+                            out[e] = v;
                         }
                     }
                 }
             } else {
-                // rows: through the staging tile, lanes 8r .. 8r+7 on 8 outputs of row r;
-                // two 8-output chunks a round, their 16 stage-start loads issued first
+                // rows: through the staging tile, lanes 8r .. 8r+7 on 8 outputs of row r
 #pragma unroll
-                for (int c0 = 0; c0 < toe::N; c0 += 16) {
+                for (int c0 = 0; c0 < toe::N; c0 += 8) {
                     if (c0 >= nout) continue;   // warp-uniform
-                    float pv[16];
-                    const float* rowp = prev + fo + (long long)(job.first + 32 * warp + (lane >> 3)) * fp + (lane & 7);
 #pragma unroll
-                    for (int h = 0; h < 2; h++)
+                    for (int q = 0; q < 8; q++) st[lane * STG + q] = d[c0 + q];
+                    __syncwarp();
 #pragma unroll
-                        for (int k = 0; k < 8; k++) {
-                            const int x = 8 * h + k, i = c0 + 8 * h + (lane & 7), sr = 32 * warp + 4 * k + (lane >> 3);
-                            pv[x] = (sr < job.count && i < nout) ? rowp[(long long)(4 * k) * fp + c0 + 8 * h] : 0.f;
+                    for (int k = 0; k < 8; k++) {
+                        const int r = 4 * k + (lane >> 3), q = lane & 7, i = c0 + q, sr = 32 * warp + r;
+                        if (sr < job.count && i < nout) {
+                            const long long e = fo + (long long)(job.first + sr) * fp + i;
+                            float v = rk_update(prev[e], st[r * STG + q], vel, cdt, rho, c2, rinv);
+                            if (att) v = __fmul_rn(v, A.att[ao + i]);
+                            out[e] = v;
                         }
-#pragma unroll
-                    for (int h = 0; h < 2; h++) {
-                        const int cc = c0 + 8 * h;
-                        if (cc >= nout) continue;   // warp-uniform
-#pragma unroll
-                        for (int q = 0; q < 8; q++) st[lane * STG + q] = d[cc + q];
-                        __syncwarp();
-#pragma unroll
-                        for (int k = 0; k < 8; k++) {
-                            const int x = 8 * h + k, r = 4 * k + (lane >> 3), q = lane & 7, sr = 32 * warp + r;
-                            if (sr < job.count && cc + q < nout) {
-                                float v = rk_update(pv[x], st[r * STG + q], vel, cdt, rho, c2, rinv);
-                                if (att) v = __fmul_rn(v, A.att[ao + cc + q]);
-                                out[fo + (long long)(job.first + sr) * fp + cc + q] = v;
-                            }
-                        }
-                        __syncwarp();
                     }
+                    __syncwarp();
                 }
             }
             ++g;
